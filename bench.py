@@ -1,0 +1,379 @@
+"""Benchmark: NMF iterations/s on one GB300 (or N independent replicas).
+
+Workload (the headline): multiplicative-update Euclidean NMF, V 8192 x 8192
+FP32 = A B + |N(0, 0.01)| with A 8192x64, B 64x8192 ~ Gamma(2, 0.5) (seed 2),
+r = 64, W/H U[0,1)+1e-4 (seed 3), eps 1e-9.  A step is one NMF iteration
+(H update then W update).  V is 268 MB in FP32 (134 MB as BF16), larger than
+the 129 MB L2, so consecutive steps stream it from HBM; no flush is added.
+
+Arms:
+  ours (default)     the engine through its C ABI; `value` is device-timed
+                     (CUDA events on the job's stream, inputs resident);
+                     `e2e` is the same job through the public API from pinned
+                     host buffers: create (H2D of V, W, H), K iterations with
+                     the per-iteration quality read-back of the reference's
+                     DoIteration, then GetW/GetH (D2H), all inside the timed
+                     region.
+  --impl reference   the reference's CPU NMF (HostNMF.h:64-114) on the host
+                     cores: the oracle's transcription (or the reference's
+                     own build where present), all host threads.  Each step
+                     is one iteration of the same rule on a 128-column slice
+                     of the same V (W full, H sliced), scaled to full-size
+                     iterations by the ratio of their multiply-add counts.
+
+Multi-GPU: the path does not shard (one factorisation per GPU), so --gpus N
+runs N independent replicas (one per rank, launched by torchrun) and reports
+the summed iterations/s over the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+FALLBACK_BF16_TFLOPS = 1900.0
+
+METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
+
+# DRAM bytes per launch of the dominant kernel from the committed ncu capture
+# (profiles/ncu_<kernel>_*.txt); None until a capture of that kernel exists.
+NCU_TRAFFIC_PER_LAUNCH = {"bf16": None, "fp32": None}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["bf16", "fp32"], default=None)
+    p.add_argument("--n", type=int, default=8192)
+    p.add_argument("--m", type=int, default=8192)
+    p.add_argument("--r", type=int, default=64)
+    p.add_argument("--full-job-iters", type=int, default=500,
+                   help="iterations of the residual comparison job (0 = skip)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for replicas (gloo on the host; no data-path collective)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, FALLBACK_BF16_TFLOPS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.error = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception as e:  # no nvidia-smi
+            self.error = str(e)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if self.error or not self.lines:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                    "note": self.error or "no samples"}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# reference arm / CPU baseline
+# ---------------------------------------------------------------------------
+
+def euclid_madds(n, m, r):
+    # W'V, W'W, W'W H, V H', H H', W H H'  (multiply-adds)
+    return 2 * n * m * r + r * r * n + r * r * m + r * r * m + n * r * r + n * r * r
+
+
+def cpu_reference_steps(V, W, H, r, steps, warmup, slice_cols=128):
+    """Time the reference CPU iteration on a column slice; returns (iters/s full-size, info)."""
+    import oracle
+    n, m = V.shape
+    mc = min(slice_cols, m)
+    Vs = np.asfortranarray(V[:, :mc])
+    Hs = np.asfortranarray(H[:, :mc])
+    threads = os.cpu_count() or 1
+    use_ref = oracle.ref() is not None
+    kind = "reference" if use_ref else "port"
+    Wc, Hc = W.copy(order="F"), Hs.copy(order="F")
+
+    def one():
+        nonlocal Wc, Hc
+        if use_ref:
+            # the reference build is single-threaded (HostNMF has no threading)
+            Wc, Hc = oracle.reference_run(0, Vs, Wc, Hc, 1)
+        else:
+            Wc, Hc = oracle.hostnmf_run(0, Vs, Wc, Hc, 1, eps=np.float32(1e-9), nthreads=threads)
+
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    dt = time.perf_counter() - t0
+    scale = euclid_madds(n, mc, r) / euclid_madds(n, m, r)
+    ips = steps * scale / dt
+    info = {"kind": kind, "cores": 1 if use_ref else threads,
+            "sample": "%d iterations of the %dx%d slice (r=%d) of V; scaled by multiply-adds %.5f of a full "
+                      "%dx%d iteration" % (steps, n, mc, r, scale, n, m),
+            "seconds": dt}
+    return ips, info
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def make_workload(n, m, r):
+    from gpumlib_gb300 import inputs
+    cfg = inputs.large_euclidean(n, m, r)
+    return cfg["V"], cfg["W"], cfg["H"], cfg["eps"]
+
+
+def run_ours(args, rank, world, local, dist):
+    import gpumlib_gb300 as g
+    from gpumlib_gb300 import _native
+
+    lib = _native.load()
+    if g.device_count() < 1:
+        raise RuntimeError("no CUDA device")
+    precision = args.precision or "bf16"
+    n, m, r = args.n, args.m, args.r
+    V, W, H, eps = make_workload(n, m, r)
+    try:
+        nmf = g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=precision, quality_interval=0)
+    except g.GpuNmfError as e:
+        if precision == "bf16" and e.status == 4:
+            precision = "fp32"
+            nmf = g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=precision, quality_interval=0)
+        else:
+            raise
+    # warm-up, then the timed steps
+    nmf.Iterate(args.warmup)
+    nmf.Synchronize()
+    dist.barrier()
+    with ClockSampler(local) as clk:
+        t = nmf.TimeIterations(args.steps, kernel_timing=True)
+    ms = dist.max(t["total_ms"])
+    value = world * args.steps / (ms / 1e3)
+    nmf.close()
+
+    # roofline of the dominant kernel (the V-streaming product)
+    hbm, _, src = peaks()
+    vbytes = 2 if precision == "bf16" else 4
+    per_launch_bytes = n * m * vbytes + (n * r + r * m) * vbytes + (r * m if precision != "bf16" else 0) * 4
+    kl = max(1, t["kernel_launches"])
+    avg_ms = t["kernel_ms"] / kl
+    achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
+    traffic = NCU_TRAFFIC_PER_LAUNCH.get(precision)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": src,
+                "kernel": "V-streaming product (W'V / VH')", "avg_launch_ms": round(avg_ms, 5),
+                "algorithmic_bytes_per_launch": per_launch_bytes}
+
+    out = {"metric": METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if precision == "bf16" else "f32",
+           "data": "synthetic: V = A B + |N(0,0.01)|, A,B ~ Gamma(2,0.5) (seed 2); W,H U[0,1)+1e-4 (seed 3)",
+           "config": {"workload": "large_euclidean_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r,
+                      "rule": "euclidean", "precision": precision, "eps": eps,
+                      "parallelism": "replicas" if world > 1 else "single",
+                      "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16 > 129 MB); no flush" %
+                            (n * m * 4 >> 20, n * m * 2 >> 20)},
+           "clocks": clk.summary(), "gpu_launches": t["launches"], "roofline": roofline}
+
+    # end to end through the public API from pinned host buffers
+    if not args.no_e2e:
+        out["e2e"] = run_e2e(lib, g, V, W, H, eps, precision, args, dist, world)
+
+    # equal-residual check: a full job in each precision
+    if args.full_job_iters and rank == 0:
+        res = {}
+        for prec in (["bf16", "fp32"] if precision == "bf16" else ["fp32"]):
+            with g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=prec, quality_interval=0) as j:
+                tt = j.TimeIterations(args.full_job_iters)
+                res[prec] = {"residual": j.Residual(), "iters_per_s": round(args.full_job_iters / (tt["total_ms"] / 1e3), 2)}
+        out["full_job"] = {"iters": args.full_job_iters, **res}
+        if "bf16" in res:
+            out["full_job"]["residual_gap"] = abs(res["bf16"]["residual"] - res["fp32"]["residual"])
+            out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 3)
+
+    if rank == 0 and not args.no_cpu_baseline:
+        ips, info = cpu_reference_steps(V, W, H, r, steps=3, warmup=1)
+        out["cpu_baseline"] = {"value": ips, "unit": "iters/s", **info}
+    return out
+
+
+def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world):
+    import ctypes
+    n, m = V.shape
+    r = W.shape[1]
+    bufs = []
+    try:
+        def pinned(a):
+            p = lib.gpunmf_host_alloc(a.nbytes)
+            if not p:
+                raise MemoryError("pinned allocation failed")
+            bufs.append(p)
+            arr = np.ctypeslib.as_array((ctypes.c_float * a.size).from_address(p)).reshape(a.shape, order="F")
+            arr[...] = a
+            return arr
+        hV, hW, hH = pinned(V), pinned(W), pinned(H)
+        oW = pinned(np.zeros_like(W))
+        oH = pinned(np.zeros_like(H))
+        dist.barrier()
+        t0 = time.perf_counter()
+        nmf = g.NMF_MultiplicativeEuclidianDistance(hV, hW, hH, eps=eps, precision=precision)
+        for _ in range(args.steps):
+            nmf.DoIteration()            # per-iteration quality read-back (4 bytes D2H)
+            nmf.QualityImprovement()
+        from gpumlib_gb300 import _native
+        _native.check(lib.gpunmf_get_w(nmf._h, oW.ctypes.data_as(ctypes.c_void_p)))
+        _native.check(lib.gpunmf_get_h(nmf._h, oH.ctypes.data_as(ctypes.c_void_p)))
+        dt = time.perf_counter() - t0
+        nmf.close()
+        dt = dist.max(dt)
+        h2d = V.nbytes + W.nbytes + H.nbytes
+        d2h = W.nbytes + H.nbytes + 4 * args.steps
+        return {"value": round(world * args.steps / dt, 2), "unit": "iters/s",
+                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+                "note": "one job of %d iterations from pinned host buffers: create (H2D V,W,H), iterations with "
+                        "quality read-back, GetW/GetH (D2H); bytes amortised per step" % args.steps}
+    finally:
+        for p in bufs:
+            lib.gpunmf_host_free(p)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    n, m, r = args.n, args.m, args.r
+    V, W, H, eps = make_workload(n, m, r)
+    ips, info = cpu_reference_steps(V, W, H, r, steps=max(1, args.steps), warmup=max(0, min(args.warmup, 2)))
+    return {"impl": "reference", "metric": METRIC, "value": ips, "unit": "iters/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / ips if ips else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (same workload as the engine arm)",
+            "config": {"workload": "large_euclidean_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r,
+                       "rule": "euclidean", "precision": "fp32"},
+            "cpu_baseline": {"value": ips, "unit": "iters/s", **info},
+            "e2e": {"value": ips, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out))
+        return 0
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    dist = Dist(world)
+    try:
+        out = run_ours(args, rank, world, local, dist)
+    finally:
+        dist.close()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

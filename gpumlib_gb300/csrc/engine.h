@@ -1,0 +1,67 @@
+// Internal job structure shared by the engine and the tensor-core path.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/gpunmf.h"
+
+struct TcState;  // tensor-core path state (tc_kernels.cu)
+
+struct gpunmf_job {
+    int rule = 0, n = 0, m = 0, r = 0, precision = 0;
+    float eps = 1e-8f;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+
+    // FP32 master copies, column-major (V n x m, W n x r, H r x m)
+    float *V = nullptr, *W = nullptr, *H = nullptr;
+
+    // FP32-path workspaces
+    int s_h = 1, s_w = 1, s_g = 1;            // split-K slices
+    float *P_h = nullptr, *P_w = nullptr;     // split-K partial products of the H- and W-steps
+    float *P_g = nullptr, *G = nullptr;       // Gram partials, Gram (r x r)
+    float *D_h = nullptr, *D_w = nullptr;     // W'W H (r x m) and W H H' (n x r)
+    float *WH = nullptr;                      // n x m (KL; lazily for GetWH)
+    float *sums = nullptr;                    // r (KL column/row sums)
+    double *red = nullptr;                    // per-CTA FP64 partials
+    size_t red_cap = 0;
+    float *d_quality = nullptr;
+    double *d_scalar = nullptr;
+    unsigned char *h_pinned = nullptr;        // 64 pinned bytes: quality (float) at 0, scalar (double) at 8
+    float *h_quality() { return reinterpret_cast<float *>(h_pinned); }
+    double *h_scalar() { return reinterpret_cast<double *>(h_pinned + 8); }
+
+    // quality bookkeeping (src/algorithms/nmf/nmf_base.h:49-53)
+    int q_interval = 1;
+    int q_times = 0;
+    float q_last = -1.0f, q_delta = 1.0f;
+    bool q_pending = false;
+    cudaEvent_t qev = nullptr;
+    long long iter_count = 0;
+
+    // launch accounting and optional per-kernel timing
+    long long launches = 0;
+    bool timing = false;
+    int timed_launches = 0;
+    std::vector<cudaEvent_t> tev;
+
+    TcState *tc = nullptr;
+};
+
+namespace gpunmf {
+void mark_begin(gpunmf_job *j);
+void mark_end(gpunmf_job *j);
+gpunmf_status job_quality_step(gpunmf_job *j, bool fused_wh);
+size_t job_footprint(int rule, int n, int m, int r, int precision);
+
+// tensor-core path (tc_kernels.cu)
+gpunmf_status tc_supported(int rule, int n, int m, int r);
+void tc_add_sizes(int rule, int n, int m, int r, size_t *red_doubles);
+size_t tc_footprint(int rule, int n, int m, int r);
+gpunmf_status tc_create(gpunmf_job *j);
+gpunmf_status tc_prepare(gpunmf_job *j);  // after V/W/H are uploaded
+gpunmf_status tc_iterate(gpunmf_job *j, bool updateW);
+void tc_destroy(gpunmf_job *j);
+}  // namespace gpunmf

@@ -1,0 +1,203 @@
+/*
+ * gpunmf.h — C ABI of the GB300 multiplicative-update NMF engine.
+ *
+ * Plain C: pointers, sizes and status codes only.  Every matrix at this
+ * boundary is FP32 and column-major, exactly as GPUMLib requires of its
+ * callers (src/algorithms/nmf/nmf_base.h:92,109-114):
+ *   V  n x m   (element (i,u) at V[u*n + i])
+ *   W  n x r   (element (i,a) at W[a*n + i])
+ *   H  r x m   (element (a,u) at H[u*r + a])
+ *
+ * Two layers are exported:
+ *
+ *  1. Job API (gpunmf_*): what GPUMLib's NMF classes do
+ *     (src/algorithms/nmf/nmf_base.h:45-151,
+ *      nmf_multiplicative_euclidian.{h,cpp}, nmf_multiplicative_divergence.{h,cpp}),
+ *     as an opaque handle that owns the device copies of V, W and H.
+ *     include/gpumlib_nmf.hpp wraps it in the reference's C++ classes.
+ *
+ *  2. Kernel API (gpumlib_cuda_nmf_*, gpumlib_nmf_*): the reference's
+ *     extern "C" launch wrappers of src/cuda/nmf/nmf_kernels.h:87,100,113 with
+ *     the same names and arguments, plus C entry points for its C++-linkage
+ *     helpers KernelSumW / KernelSumH / KernelNMFquality
+ *     (nmf_kernels.h:44,64,73).  They take device pointers, launch on the
+ *     legacy default stream like the reference, and return the launch's
+ *     cudaError_t (as int).
+ *
+ * Status codes: every gpunmf_* call returns gpunmf_status.  Nothing is
+ * printed and nothing aborts; a CUDA failure is reported as GPUNMF_ERR_CUDA
+ * and its text is kept for gpunmf_last_error().
+ */
+#ifndef GPUNMF_H
+#define GPUNMF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GPUNMF_OK = 0,
+    GPUNMF_ERR_INVALID = 1,      /* bad handle, shape, pointer or option  */
+    GPUNMF_ERR_CUDA = 2,         /* a CUDA call failed (see last_error)   */
+    GPUNMF_ERR_NOMEM = 3,        /* device or pinned allocation failed    */
+    GPUNMF_ERR_UNSUPPORTED = 4,  /* option not available for this job     */
+    GPUNMF_ERR_NO_DEVICE = 5,    /* no CUDA device, or not an sm_103 GPU   */
+    GPUNMF_ERR_TIMEOUT = 6,      /* a bounded device wait gave up         */
+    GPUNMF_ERR_REJECTED = 7      /* admission control refused a job       */
+} gpunmf_status;
+
+/* Update rules (GPUMLib class names in brackets). */
+typedef enum {
+    GPUNMF_EUCLIDEAN = 0,   /* NMF_MultiplicativeEuclidianDistance */
+    GPUNMF_DIVERGENCE = 1   /* NMF_MultiplicativeDivergence (KL)   */
+} gpunmf_rule;
+
+/* Arithmetic of the factor products.  The W/H update itself is always FP32. */
+typedef enum {
+    GPUNMF_FP32 = 0,        /* plain FP32 (CUDA cores): the drop-in path         */
+    GPUNMF_BF16 = 1         /* BF16 tensor-core products (tcgen05), FP32 accumulate */
+} gpunmf_precision;
+
+typedef struct gpunmf_job *gpunmf_handle;
+
+/* Reference epsilon: SMALL_VALUE_TO_ADD_DENOMINATOR = 10e-9 (nmf_kernels.h:34). */
+#define GPUNMF_REFERENCE_EPS 1e-8f
+
+/* Text of the last error on this thread ("" if none). */
+const char *gpunmf_last_error(void);
+
+/* Library version string. */
+const char *gpunmf_version(void);
+
+/* Number of CUDA devices visible (0 when none). */
+int gpunmf_device_count(void);
+
+/*
+ * Create a job from HOST matrices (copied to the device), like
+ * NMF(v, w, h) (nmf_base.h:108-120).  W and H are the initial factors.
+ * stream: a cudaStream_t (NULL = the library creates its own stream).
+ * eps: denominator guard; GPUNMF_REFERENCE_EPS reproduces the reference.
+ */
+gpunmf_status gpunmf_create(int rule, int n, int m, int r,
+                            const float *V, const float *W, const float *H,
+                            float eps, int precision, void *stream,
+                            gpunmf_handle *out);
+
+/*
+ * Create a job like NMF(v, r) (nmf_base.h:91-106): W and H are drawn on the
+ * host as uniform[0,1) + eps from a counter-based generator keyed by seed
+ * (the reference draws them from an unseeded rand()).
+ */
+gpunmf_status gpunmf_create_random(int rule, int n, int m, int r, const float *V,
+                                   unsigned long long seed, float eps, int precision,
+                                   void *stream, gpunmf_handle *out);
+
+/* Same as gpunmf_create but V, W, H are DEVICE pointers (copied on the job's stream). */
+gpunmf_status gpunmf_create_device(int rule, int n, int m, int r,
+                                   const float *dV, const float *dW, const float *dH,
+                                   float eps, int precision, void *stream,
+                                   gpunmf_handle *out);
+
+gpunmf_status gpunmf_destroy(gpunmf_handle h);
+
+/*
+ * Run `iters` iterations of DoIteration(updateW) (nmf_base.h:145).
+ * Order per iteration: H first, then (if updateW) W with the new H.
+ * Enqueued on the job's stream; returns without waiting for the GPU.
+ */
+gpunmf_status gpunmf_iterate(gpunmf_handle h, int iters, int updateW);
+
+/*
+ * Quality bookkeeping of DetermineQualityImprovement (nmf_base.h:70-89).
+ * interval k > 0: the log10 quality is evaluated every k-th iteration
+ * (1 = every iteration, the reference's behaviour when its GPU keeps up);
+ * 0 turns it off.  Default: 1.
+ */
+gpunmf_status gpunmf_set_quality_interval(gpunmf_handle h, int interval);
+
+/* QualityImprovement() (nmf_base.h:148-150): lagged change of the quality; 1.0 initially. */
+gpunmf_status gpunmf_quality_improvement(gpunmf_handle h, float *out);
+
+/* Relative Frobenius residual ||V - W H||_F / ||V||_F of the current factors,
+ * WH in FP32 from the FP32 factors, squares accumulated in FP64 on the GPU. */
+gpunmf_status gpunmf_residual_fp64(gpunmf_handle h, double *out);
+
+/* Generalised KL objective sum V log(V/WH) - V + WH (FP64 on the GPU). */
+gpunmf_status gpunmf_objective_kl_fp64(gpunmf_handle h, double *out);
+
+/* GetW / GetH / GetWH (nmf_base.h:125-141): synchronous copies to host
+ * buffers of n*r, r*m and n*m floats, column-major. */
+gpunmf_status gpunmf_get_w(gpunmf_handle h, float *W);
+gpunmf_status gpunmf_get_h(gpunmf_handle h, float *H);
+gpunmf_status gpunmf_get_wh(gpunmf_handle h, float *WH);
+
+/* Device pointers of the job's FP32 factors (valid until destroy). */
+gpunmf_status gpunmf_device_factors(gpunmf_handle h, float **dW, float **dH);
+
+/* Wait for the job's queued work. */
+gpunmf_status gpunmf_synchronize(gpunmf_handle h);
+
+/* Shape/options of a job. */
+gpunmf_status gpunmf_info(gpunmf_handle h, int *rule, int *n, int *m, int *r,
+                          int *precision, float *eps);
+
+/* Device bytes a job of this shape holds (admission accounting). */
+size_t gpunmf_footprint_bytes(int rule, int n, int m, int r, int precision);
+
+/* Host-only: out[k] = uniform[0,1) value number offset+k of the counter-based
+ * generator keyed by seed (the generator gpunmf_create_random uses). */
+void gpunmf_fill_uniform(unsigned long long seed, unsigned long long offset, size_t count, float *out);
+
+/* Page-locked host buffers for end-to-end transfers (NULL on failure). */
+void *gpunmf_host_alloc(size_t bytes);
+void gpunmf_host_free(void *p);
+
+/*
+ * Timing helper: enqueue `iters` iterations bracketed by CUDA events on the
+ * job's stream, wait, and return the elapsed milliseconds.  When
+ * kernel_ms/kernel_launches are given, the two V-streaming kernels of each
+ * iteration are also bracketed by events and their summed device time and
+ * launch count are returned (for the roofline of the dominant kernel).
+ */
+gpunmf_status gpunmf_time_iterations(gpunmf_handle h, int iters, int updateW,
+                                     float *total_ms, float *kernel_ms,
+                                     int *kernel_launches, int *all_launches);
+
+/* ------------------------------------------------------------------ */
+/* Kernel API: same names and arguments as src/cuda/nmf/nmf_kernels.h. */
+/* gridDim/blockDim are accepted for source compatibility; the GB300   */
+/* kernels pick their own launch shape (vectorised, grid-stride).      */
+/* Return value: cudaError_t of the launch (0 = cudaSuccess).          */
+/* ------------------------------------------------------------------ */
+typedef struct { unsigned int x, y, z; } gpunmf_dim3;   /* layout of CUDA's dim3 */
+
+/* nmf_kernels.h:87 — m[i] *= nm[i] / (dm[i] + 1e-8), i < elements */
+int gpumlib_cuda_nmf_multiplicative_euclidean_update_matrix(
+    unsigned int gridDim, unsigned int blockDim, float *nm, float *dm, float *m, int elements);
+
+/* nmf_kernels.h:100 — W(i,a) *= [sum_u H(a,u) V(i,u)/(WH(i,u)+1e-8)] / sumH[a] */
+int gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_w(
+    gpunmf_dim3 gridDim, gpunmf_dim3 blockDim, float *W, float *H, float *V, float *WH,
+    float *sumH, int n, int m, int r);
+
+/* nmf_kernels.h:113 — H(a,u) *= [sum_i W(i,a) V(i,u)/(WH(i,u)+1e-8)] / sumW[a] */
+int gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_h(
+    gpunmf_dim3 gridDim, gpunmf_dim3 blockDim, float *H, float *W, float *V, float *WH,
+    float *sumW, int n, int m, int r);
+
+/* nmf_kernels.h:64 (KernelSumW) — sumW[a] = max(sum_i W(i,a), 1e-8) */
+int gpumlib_nmf_sum_w(int blockSize, float *W, int n, int r, float *sumW);
+
+/* nmf_kernels.h:73 (KernelSumH) — sumH[a] = max(sum_u H(a,u), 1e-8) */
+int gpumlib_nmf_sum_h(int blockSize, float *H, int r, int m, float *sumH);
+
+/* nmf_kernels.h:44 (KernelNMFquality) — *quality = sum_k V[k] log10(WH[k]+1e-8) - WH[k] */
+int gpumlib_nmf_quality(int blockSize, float *V, float *WH, int n, float *quality);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUNMF_H */

@@ -1,0 +1,146 @@
+"""ctypes access to the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this package, and only as the checker.  ``orc()`` loads the float/double
+restatement built from oracle/nmf_oracle.c; ``ref()`` loads the reference's
+own HostNMF built from its sources (present only where the reference tree
+was available at build time).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_orc = None
+_ref = None
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def orc():
+    global _orc
+    if _orc is None:
+        path = os.path.join(_build.LIB_DIR, "liborc.so")
+        if not os.path.exists(path):
+            path = _build.build_oracle()
+        lib = ctypes.CDLL(path)
+        vp, i, f, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
+        lib.orc_hostnmf_me_iter.argtypes = [i, i, i, vp, vp, vp, i, f, vp, i]
+        lib.orc_hostnmf_md_iter.argtypes = [i, i, i, vp, vp, vp, i, f, i, vp, i]
+        lib.orc_hostnmf_wh.argtypes = [i, i, i, vp, vp, vp, i]
+        lib.orc_f64_me_iter.argtypes = [i, i, i, vp, vp, vp, i, d, vp, i]
+        lib.orc_f64_md_iter.argtypes = [i, i, i, vp, vp, vp, i, d, vp, i]
+        lib.orc_f64_md_iter.restype = i
+        lib.orc_quality.argtypes = [ctypes.c_long, vp, vp, f]
+        lib.orc_quality.restype = d
+        lib.orc_residual.argtypes = [i, i, i, vp, vp, vp, i]
+        lib.orc_residual.restype = d
+        _orc = lib
+    return _orc
+
+
+def ref():
+    """The reference's HostNMF library, or None when it was not built here."""
+    global _ref
+    if _ref is None:
+        path = os.path.join(_build.REF_DIR, "libhostnmf_ref.so")
+        if not os.path.exists(path):
+            if not _build.reference_available():
+                return None
+            path = _build.build_ref()
+        lib = ctypes.CDLL(path)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        lib.ref_hostnmf_run.argtypes = [i, i, i, i, vp, vp, vp, i, i, vp]
+        lib.ref_hostnmf_run.restype = i
+        lib.ref_hostnmf_time.argtypes = [i, i, i, i, vp, vp, vp, i]
+        lib.ref_hostnmf_time.restype = ctypes.c_double
+        _ref = lib
+    return _ref
+
+
+def _f32(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float32)).copy(order="F")
+
+
+def hostnmf_run(rule, V, W, H, iters, updateW=True, eps=1e-8, clamp_sums=False, nthreads=1,
+                residuals=False):
+    """Float transcription of HostNMF (rule 0 Euclidean, 1 KL); returns (W, H[, resid])."""
+    lib = orc()
+    V = _f32(V); W = _f32(W); H = _f32(H)
+    n, m = V.shape
+    r = W.shape[1]
+    if rule == 0:
+        ws = np.empty(2 * r * m + r * r + 2 * n * r, dtype=np.float32)
+    else:
+        ws = np.empty(n * m, dtype=np.float32)
+    res = []
+    for _ in range(iters):
+        if rule == 0:
+            lib.orc_hostnmf_me_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, _p(ws), nthreads)
+        else:
+            lib.orc_hostnmf_md_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, int(clamp_sums),
+                                    _p(ws), nthreads)
+        if residuals:
+            res.append(residual(V, W, H, nthreads))
+    return (W, H, np.array(res)) if residuals else (W, H)
+
+
+def f64_run(rule, V, W, H, iters, updateW=True, eps=1e-8, nthreads=1):
+    """Double-precision GPU-semantics rules; returns float64 (W, H)."""
+    lib = orc()
+    V = np.asfortranarray(np.asarray(V, dtype=np.float64))
+    W = np.asfortranarray(np.asarray(W, dtype=np.float64)).copy(order="F")
+    H = np.asfortranarray(np.asarray(H, dtype=np.float64)).copy(order="F")
+    n, m = V.shape
+    r = W.shape[1]
+    if rule == 0:
+        ws = np.empty(2 * r * m + r * r + 2 * n * r, dtype=np.float64)
+    else:
+        ws = np.empty(n * m + r, dtype=np.float64)
+    for _ in range(iters):
+        if rule == 0:
+            lib.orc_f64_me_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, _p(ws), nthreads)
+        else:
+            if lib.orc_f64_md_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, _p(ws), nthreads) != 0:
+                raise ValueError("r too large for the oracle")
+    return W, H
+
+
+def hostnmf_wh(W, H, nthreads=1):
+    W = _f32(W); H = _f32(H)
+    n, r = W.shape
+    m = H.shape[1]
+    WH = np.empty((n, m), dtype=np.float32, order="F")
+    orc().orc_hostnmf_wh(n, m, r, _p(W), _p(H), _p(WH), nthreads)
+    return WH
+
+
+def quality(V, WH, eps=1e-8):
+    V = _f32(V); WH = _f32(WH)
+    return orc().orc_quality(V.size, _p(V), _p(WH), eps)
+
+
+def residual(V, W, H, nthreads=1):
+    V = _f32(V); W = _f32(W); H = _f32(H)
+    n, m = V.shape
+    return orc().orc_residual(n, m, W.shape[1], _p(V), _p(W), _p(H), nthreads)
+
+
+def reference_run(rule, V, W, H, iters, updateW=True, residuals=False):
+    """Run the reference's own HostNMF (built from its sources); None if unavailable."""
+    lib = ref()
+    if lib is None:
+        return None
+    V = _f32(V); W = _f32(W); H = _f32(H)
+    n, m = V.shape
+    r = W.shape[1]
+    res = np.zeros(iters, dtype=np.float64)
+    rc = lib.ref_hostnmf_run(rule, n, m, r, _p(V), _p(W), _p(H), iters, int(updateW),
+                             _p(res) if residuals else None)
+    if rc != 0:
+        raise RuntimeError("ref_hostnmf_run failed")
+    return (W, H, res) if residuals else (W, H)

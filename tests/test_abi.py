@@ -1,0 +1,136 @@
+"""The C ABI library loads and exports every function the public headers declare.
+
+No compute call is made here (the CPU suite runs without a GPU); create-type
+calls are only checked for their error status when no device is visible.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in sorted(os.listdir(os.path.join(ROOT, "include")))
+           if f.endswith(".h")]
+
+
+def declared_functions():
+    names = []
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for mt in re.finditer(r"\b((?:gpunmf|gpumlib)_\w+)\s*\(", text):
+            names.append(mt.group(1))
+    return sorted(set(names))
+
+
+def test_headers_declare_functions():
+    names = declared_functions()
+    assert "gpunmf_create" in names and "gpumlib_cuda_nmf_multiplicative_euclidean_update_matrix" in names
+
+
+def test_library_exports_every_declared_symbol(built):
+    from gpumlib_gb300 import _native
+    lib = _native.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", _native.lib_path()], capture_output=True, text=True)
+    exported = set(l.split()[-1] for l in out.stdout.splitlines() if l.strip())
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, "declared but not exported: %s" % missing
+    bound = set(s[0] for s in _native.SIGNATURES)
+    unbound = [n for n in declared_functions() if n not in bound]
+    assert not unbound, "declared but without a ctypes signature: %s" % unbound
+    for n in declared_functions():
+        getattr(lib, n)
+
+
+def test_version_and_host_only_calls(built):
+    from gpumlib_gb300 import _native, inputs
+    lib = _native.load()
+    assert b"sm_103a" in lib.gpunmf_version()
+    out = np.empty(1000, dtype=np.float32)
+    lib.gpunmf_fill_uniform(7, 123, out.size, out.ctypes.data_as(ctypes.c_void_p))
+    assert np.array_equal(out, inputs.uniform(7, 1000, offset=123))
+    assert lib.gpunmf_footprint_bytes(0, 8192, 8192, 64, 0) > 8192 * 8192 * 4
+    assert lib.gpunmf_footprint_bytes(0, 0, 10, 2, 0) == 0
+
+
+def test_null_handle_errors(built):
+    from gpumlib_gb300 import _native
+    lib = _native.load()
+    assert lib.gpunmf_iterate(None, 1, 1) == 1
+    assert lib.gpunmf_destroy(None) == 1
+    assert b"null" in lib.gpunmf_last_error()
+
+
+def test_create_without_gpu_reports_no_device(built):
+    from gpumlib_gb300 import _native
+    lib = _native.load()
+    if lib.gpunmf_device_count() > 0:
+        pytest.skip("a GPU is visible")
+    V = np.ones((4, 3), dtype=np.float32, order="F")
+    W = np.ones((4, 2), dtype=np.float32, order="F")
+    H = np.ones((2, 3), dtype=np.float32, order="F")
+    h = ctypes.c_void_p()
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    st = lib.gpunmf_create(0, 4, 3, 2, p(V), p(W), p(H), 1e-8, 0, None, ctypes.byref(h))
+    assert st == 5  # GPUNMF_ERR_NO_DEVICE
+    assert st == lib.gpunmf_create(0, 4, 3, 2, p(V), p(W), p(H), 1e-8, 0, None, ctypes.byref(h))
+
+
+def test_invalid_arguments_rejected_before_device(built):
+    from gpumlib_gb300 import _native
+    lib = _native.load()
+    h = ctypes.c_void_p()
+    V = np.ones((4, 3), dtype=np.float32, order="F")
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.gpunmf_create(9, 4, 3, 2, p(V), p(V), p(V), 1e-8, 0, None, ctypes.byref(h)) == 1
+    assert lib.gpunmf_create(0, 4, 3, 0, p(V), p(V), p(V), 1e-8, 0, None, ctypes.byref(h)) == 1
+    assert lib.gpunmf_create(0, 4, 3, 2, None, p(V), p(V), 1e-8, 0, None, ctypes.byref(h)) == 1
+    assert lib.gpunmf_create(0, 4, 3, 2, p(V), p(V), p(V), -1.0, 0, None, ctypes.byref(h)) == 1
+    assert lib.gpunmf_create(0, 4, 3, 2, p(V), p(V), p(V), 1e-8, 7, None, ctypes.byref(h)) == 1
+
+
+def test_cpp_dropin_header_compiles(built, tmp_path):
+    """A FacesNMF-style caller compiles against include/gpumlib_nmf.hpp and links the library."""
+    from gpumlib_gb300 import _native
+    src = tmp_path / "caller.cpp"
+    src.write_text(CPP_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_native.lib_path())
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    r = subprocess.run(["g++", "-std=c++14", "-O1", "-I", os.path.join(ROOT, "include"), "-I", cuda + "/include",
+                        str(src), "-o", str(exe), "-L", libdir, "-lgpunmf", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+CPP_CALLER = r"""
+#include <cstdio>
+#include "gpumlib_nmf.hpp"
+using namespace GPUMLib;
+int main() {
+    int n = 40, m = 30, r = 4;
+    HostMatrix<cudafloat> V(n, m, ColumnMajor), W(n, r, ColumnMajor), H(r, m, ColumnMajor);
+    for (int j = 0; j < m; j++) for (int i = 0; i < n; i++) V(i, j) = (float)((i * 7 + j * 3) % 11) / 11.0f;
+    for (int a = 0; a < r; a++) for (int i = 0; i < n; i++) W(i, a) = 0.5f + 0.01f * ((i + a) % 5);
+    for (int j = 0; j < m; j++) for (int a = 0; a < r; a++) H(a, j) = 0.5f + 0.01f * ((j + a) % 7);
+    try {
+        NMF_MultiplicativeEuclidianDistance nmf(V, W, H);
+        NMF * p = &nmf;
+        for (int it = 0; it < 50; it++) { p->DoIteration(); if (p->QualityImprovement() < 0.0001f) break; }
+        HostMatrix<cudafloat> w = p->GetW(), h = p->GetH(), wh = p->GetWH();
+        std::printf("%.9g %.9g %.9g %.12g\n", w(0, 0), h(0, 0), wh(0, 0), nmf.Residual());
+        NMF_MultiplicativeDivergence kl(V, W, H);
+        kl.DoIteration(true); kl.DoIteration(false);
+        HostMatrix<cudafloat> kw = kl.GetW();
+        std::printf("%.9g\n", kw(1, 1));
+    } catch (NMFError & e) {
+        std::printf("error %d %s\n", (int)e.status, e.what());
+        return 2;
+    }
+    return 0;
+}
+"""

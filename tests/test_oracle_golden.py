@@ -1,0 +1,75 @@
+"""The CPU oracle against golden vectors made by the reference's own HostNMF.
+
+The golden file holds W, H and per-iteration residuals produced by
+src/examples/FacesNMF/HostNMF.h compiled from the reference sources
+(tests/golden/make_golden.py).  The float transcription in
+oracle/nmf_oracle.c must reproduce them bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden.make_golden import CASES, case_inputs
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_oracle_matches_reference_bits(case, golden):
+    data, _ = golden
+    name, rule, n, m, r, iters, updateW = case[:7]
+    V, W, H = case_inputs(case)
+    Wo, Ho = oracle.hostnmf_run(rule, V, W, H, iters, updateW=updateW, eps=1e-8, nthreads=2)
+    assert np.array_equal(Wo, data[name + "/W"]), "W differs from the reference"
+    assert np.array_equal(Ho, data[name + "/H"]), "H differs from the reference"
+
+
+def test_oracle_residual_trajectory(golden):
+    data, _ = golden
+    case = [c for c in CASES if c[0] == "me_1024x512_r16"][0]
+    name, rule, n, m, r, iters, updateW = case[:7]
+    V, W, H = case_inputs(case)
+    _, _, res = oracle.hostnmf_run(rule, V, W, H, 20, updateW=updateW, eps=1e-8, nthreads=4,
+                                   residuals=True)
+    np.testing.assert_allclose(res, data[name + "/resid"][:20], rtol=1e-12)
+
+
+def test_oracle_thread_count_invariant():
+    from gpumlib_gb300 import inputs
+    V = inputs.uniform_matrix(5, 70, 45)
+    W, H = inputs.factors(6, 70, 45, 4)
+    for rule in (0, 1):
+        a = oracle.hostnmf_run(rule, V, W, H, 5, nthreads=1)
+        b = oracle.hostnmf_run(rule, V, W, H, 5, nthreads=7)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_f64_oracle_close_to_float_reference(golden):
+    """The FP64 statement of the GPU rules agrees with the float reference to rounding."""
+    data, _ = golden
+    for nm in ("me_odd_37x23_r3", "kl_odd_33x17_r5"):
+        case = [c for c in CASES if c[0] == nm][0]
+        name, rule, n, m, r, iters, updateW = case[:7]
+        V, W, H = case_inputs(case)
+        Wd, Hd = oracle.f64_run(rule, V, W, H, iters, updateW=updateW, eps=1e-8)
+        WHd = Wd @ Hd
+        WHg = data[name + "/W"].astype(np.float64) @ data[name + "/H"]
+        assert np.linalg.norm(WHd - WHg) / np.linalg.norm(WHd) < 1e-5
+
+
+def test_quality_formula():
+    V = np.array([[1.0, 2.0], [0.0, 3.0]], dtype=np.float32, order="F")
+    WH = np.array([[0.5, 1.0], [2.0, 4.0]], dtype=np.float32, order="F")
+    q = oracle.quality(V, WH, eps=1e-8)
+    exp = sum(float(v) * np.log10(float(w) + 1e-8) - float(w) for v, w in zip(V.ravel(), WH.ravel()))
+    assert abs(q - exp) < 1e-5
+
+
+def test_planted_error_is_caught(golden):
+    """A mistake planted in the oracle's inputs must break bit-equality (the check has teeth)."""
+    data, _ = golden
+    case = [c for c in CASES if c[0] == "me_odd_37x23_r3"][0]
+    name, rule, n, m, r, iters, updateW = case[:7]
+    V, W, H = case_inputs(case)
+    V = V.copy(order="F")
+    V[5, 7] = np.nextafter(V[5, 7], np.float32(2.0))
+    Wo, Ho = oracle.hostnmf_run(rule, V, W, H, iters, updateW=updateW, eps=1e-8)
+    assert not np.array_equal(Wo, data[name + "/W"])
