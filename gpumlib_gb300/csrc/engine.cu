@@ -520,7 +520,7 @@ gpunmf_status gpunmf_residual_fp64(gpunmf_handle h, double *out) {
     GPUNMF_CUDA_TRY(cudaMemcpyAsync(h->h_scalar(), h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, s));
     GPUNMF_CUDA_TRY(cudaStreamSynchronize(s));
     *out = h->h_scalar()[0];
-    return GPUNMF_OK;
+    return tc_check(h);
 }
 
 gpunmf_status gpunmf_objective_kl_fp64(gpunmf_handle h, double *out) {
@@ -547,7 +547,7 @@ gpunmf_status gpunmf_get_w(gpunmf_handle h, float *W) {
     if (!W) return GPUNMF_ERR_INVALID;
     GPUNMF_CUDA_TRY(cudaMemcpyAsync(W, h->W, sizeof(float) * (size_t)h->n * h->r, cudaMemcpyDeviceToHost, h->stream));
     GPUNMF_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return GPUNMF_OK;
+    return tc_check(h);
 }
 
 gpunmf_status gpunmf_get_h(gpunmf_handle h, float *H) {
@@ -555,7 +555,7 @@ gpunmf_status gpunmf_get_h(gpunmf_handle h, float *H) {
     if (!H) return GPUNMF_ERR_INVALID;
     GPUNMF_CUDA_TRY(cudaMemcpyAsync(H, h->H, sizeof(float) * (size_t)h->r * h->m, cudaMemcpyDeviceToHost, h->stream));
     GPUNMF_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return GPUNMF_OK;
+    return tc_check(h);
 }
 
 gpunmf_status gpunmf_get_wh(gpunmf_handle h, float *WH) {
@@ -577,7 +577,7 @@ gpunmf_status gpunmf_device_factors(gpunmf_handle h, float **dW, float **dH) {
 gpunmf_status gpunmf_synchronize(gpunmf_handle h) {
     CHECK_HANDLE(h);
     GPUNMF_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return GPUNMF_OK;
+    return tc_check(h);
 }
 
 gpunmf_status gpunmf_info(gpunmf_handle h, int *rule, int *n, int *m, int *r, int *precision, float *eps) {
@@ -622,6 +622,8 @@ gpunmf_status gpunmf_time_iterations(gpunmf_handle h, int iters, int updateW, fl
         set_error("timing failed: %s", cudaGetErrorString(ce));
         return GPUNMF_ERR_CUDA;
     }
+    if (st != GPUNMF_OK) return st;
+    st = tc_check(h);
     if (st != GPUNMF_OK) return st;
     if (total_ms) *total_ms = ms;
     if (kernel_ms) {

@@ -1,16 +1,689 @@
-// Tensor-core (tcgen05) path: placeholder until the BF16 kernels land.
+// BF16 tensor-core path (tcgen05 + TMA) of the Euclidean multiplicative update.
+//
+// Data layout in HBM (per job, beside the FP32 masters V, W, H):
+//   Vb   n x m  BF16, column-major, ld = ceil8(n)   (V itself: rows i contiguous)
+//   Vbt  m x n  BF16, column-major, ld = ceil8(m)   (V transposed: columns u contiguous)
+//   Wb   n x r  BF16, column-major, ld = ceil8(n)
+//   Hb   r x m  BF16, row-major,    ld = ceil8(m)
+// V is fixed for the whole job, so both BF16 copies are made once; with
+// them, both V-streaming products of an iteration are the same K-major x
+// K-major GEMM  D[128 x N] += A[128 x 64] B[N x 64]^T  per 64-wide K block:
+//   H-step  W'V:  rows = columns u of V,  A = Vb  tile, B = Wb, K = n
+//   W-step  VH':  rows = rows i of V,     A = Vbt tile, B = Hb, K = m
+// (src/algorithms/nmf/nmf_multiplicative_euclidian.cpp:37,56, which the
+// reference runs as cublasSgemm through DeviceMatrix.h:217-227).
+//
+// The GEMM is stream-K: every CTA (one per SM) takes an equal contiguous
+// share of the (row tile, K block) space, so the work is balanced no matter
+// how many row tiles there are.  Its share splits into at most a few
+// segments at tile boundaries; each segment's FP32 accumulator is written
+// as a partial product slot, and the update kernels (one per half-step) sum
+// the slots of a tile in a fixed order, so results are deterministic.
+//
+// Warp roles in the GEMM (192 threads, one CTA per SM):
+//   warp 0      TMA producer (one lane) + TMEM allocation
+//   warp 1      tcgen05.mma issuer (one lane)
+//   warps 2..5  epilogue: tcgen05.ld of their 32-lane TMEM quarter -> partial slot
+// Shared memory holds up to 8 stages of (A 16 KB + B N*128 B), 128-byte
+// swizzled as TMA writes them.  TMEM holds two accumulators (N columns
+// each) so the epilogue of one segment overlaps the MMAs of the next.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 #include "engine.h"
+#include "kernels.h"
+#include "tc_ptx.cuh"
 
 namespace gpunmf {
-gpunmf_status tc_supported(int, int, int, int) {
-    set_error("BF16 tensor-core path not built");
-    return GPUNMF_ERR_UNSUPPORTED;
+using namespace ptx;
+
+constexpr int kTileM = 128;
+constexpr int kBlockK = 64;
+constexpr int kGemmThreads = 192;
+constexpr int kStageABytes = kTileM * kBlockK * 2;
+constexpr int kMaxStages = 8;
+constexpr int kSmemBudget = 220 * 1024;
+constexpr int kMaxRank = 192;  // update kernels keep an r x r Gram plus two r x 33 tiles in shared memory
+
+static inline long long ceil8(long long x) { return (x + 7) / 8 * 8; }
+static inline int npad_of(int r) { return (r + 15) / 16 * 16; }
+
+struct SkParams {
+    int tiles, kblocks, npad, stages, max_seg;
+    uint32_t tmem_cols;
+    float *partials;
+    int *err;
+};
+
+extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
+
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, int *err, int bit) {
+    int ok = 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err, bit) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    return ok != 0;
 }
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    tc_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      SkParams p) {
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
+    const int stageB = p.npad * kBlockK * 2;
+    unsigned char *sA = reinterpret_cast<unsigned char *>(base);
+    unsigned char *sB = sA + p.stages * kStageABytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(sB + p.stages * stageB);
+    uint64_t *empty = full + p.stages;
+    uint64_t *tfull = empty + p.stages;  // [2]
+    uint64_t *tempty = tfull + 2;        // [2]
+    uint64_t *mdone = tempty + 2;        // [1]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long T = (long long)p.tiles * p.kblocks;
+    const long long lo = (long long)blockIdx.x * T / gridDim.x;
+    const long long hi = (long long)(blockIdx.x + 1) * T / gridDim.x;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < p.stages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 4);
+        }
+        mbar_init(mdone, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, p.tmem_cols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            tma_prefetch_desc(&tmA);
+            tma_prefetch_desc(&tmB);
+            int stage = 0;
+            uint32_t phase = 0;
+            int armed[kMaxStages];
+            for (int s = 0; s < kMaxStages; s++) armed[s] = 0;
+            for (long long b = lo; b < hi; b++) {
+                const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
+                if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty)) break;
+                mbar_arrive_expect_tx(&full[stage], kStageABytes + stageB);
+                tma_load_2d(sA + stage * kStageABytes, &tmA, kb * kBlockK, t * kTileM, &full[stage]);
+                tma_load_2d(sB + stage * stageB, &tmB, kb * kBlockK, 0, &full[stage]);
+                armed[stage]++;
+                if (++stage == p.stages) {
+                    stage = 0;
+                    phase ^= 1;
+                }
+            }
+            if (*((volatile int *)p.err) != 0) {
+                // error exit: let the copies already issued land before the CTA leaves
+                for (int s = 0; s < p.stages; s++)
+                    if (armed[s] > 0) {
+                        int dummy = 0;
+                        mbar_wait(&full[s], (uint32_t)((armed[s] - 1) & 1), &dummy, 1);
+                    }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16_f32(kTileM, p.npad);
+            int stage = 0, acc = 0;
+            uint32_t phase = 0, aphase = 0;
+            bool ok = true;
+            for (long long b = lo; b < hi && ok;) {
+                const long long t = b / p.kblocks;
+                const long long e = min(hi, (t + 1) * p.kblocks);
+                if (!mbar_wait(&tempty[acc], aphase ^ 1, p.err, kErrWaitTmemEmpty)) break;
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(acc * p.npad);
+                for (long long bb = b; bb < e; bb++) {
+                    if (!mbar_wait(&full[stage], phase, p.err, kErrWaitFull)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + stage * kStageABytes);
+                    const uint32_t b0 = smem_u32(sB + stage * stageB);
+#pragma unroll
+                    for (int k = 0; k < kBlockK / 16; k++) {
+                        tc_mma_f16(d, smem_desc(a0 + k * 32, 16, 1024, 2), smem_desc(b0 + k * 32, 16, 1024, 2),
+                                   idesc, (bb > b || k > 0) ? 1u : 0u);
+                    }
+                    tc_commit(&empty[stage]);
+                    if (++stage == p.stages) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+                if (!ok) break;
+                tc_commit(&tfull[acc]);
+                if (++acc == 2) {
+                    acc = 0;
+                    aphase ^= 1;
+                }
+                b = e;
+            }
+            // all MMAs issued by this thread have completed once mdone flips
+            tc_commit(mdone);
+            int dummy = 0;
+            mbar_wait(mdone, 0, &dummy, 1);
+        }
+    } else {
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        int acc = 0, seg = 0;
+        uint32_t aphase = 0;
+        for (long long b = lo; b < hi;) {
+            const long long t = b / p.kblocks;
+            const long long e = min(hi, (t + 1) * p.kblocks);
+            if (!warp_wait(&tfull[acc], aphase, p.err, kErrWaitTmemFull)) break;
+            tc_fence_after();
+            float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * p.npad);
+            for (int c = 0; c < p.npad; c += 16) {
+                float v[16];
+                tmem_ld16(taddr + c, v);
+                tmem_ld_wait();
+                float4 *d4 = reinterpret_cast<float4 *>(dst + c);
+                d4[0] = make_float4(v[0], v[1], v[2], v[3]);
+                d4[1] = make_float4(v[4], v[5], v[6], v[7]);
+                d4[2] = make_float4(v[8], v[9], v[10], v[11]);
+                d4[3] = make_float4(v[12], v[13], v[14], v[15]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[acc]);
+            if (++acc == 2) {
+                acc = 0;
+                aphase ^= 1;
+            }
+            seg++;
+            b = e;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, p.tmem_cols);
+    }
+}
+
+// ------------------------------------------------------------------------
+// conversions
+// ------------------------------------------------------------------------
+// V (n x m FP32 column-major) -> Vb (ld ldv) and Vbt (= V^T, ld ldvt), 32x32 tiles through shared memory
+__global__ void convert_v_kernel(const float *__restrict__ V, int n, int m, __nv_bfloat16 *__restrict__ Vb,
+                                 long long ldv, __nv_bfloat16 *__restrict__ Vbt, long long ldvt) {
+    __shared__ float tile[32][33];
+    const int i0 = blockIdx.x * 32, u0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int i = i0 + threadIdx.x, u = u0 + k;
+        float v = (i < n && u < m) ? V[(long long)u * n + i] : 0.f;
+        tile[k][threadIdx.x] = v;
+        if (i < n && u < m) Vb[(long long)u * ldv + i] = __float2bfloat16_rn(v);
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int u = u0 + threadIdx.x, i = i0 + k;
+        if (i < n && u < m) Vbt[(long long)i * ldvt + u] = __float2bfloat16_rn(tile[threadIdx.x][k]);
+    }
+}
+
+// W (n x r FP32 column-major) -> Wb (ld ldw)
+__global__ void convert_w_kernel(const float *__restrict__ W, int n, int r, __nv_bfloat16 *__restrict__ Wb,
+                                 long long ldw) {
+    long long total = (long long)n * r;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        long long a = k / n, i = k % n;
+        Wb[a * ldw + i] = __float2bfloat16_rn(W[k]);
+    }
+}
+
+// H (r x m FP32 column-major) -> Hb (r x m row-major, ld ldh)
+__global__ void convert_h_kernel(const float *__restrict__ H, int r, int m, __nv_bfloat16 *__restrict__ Hb,
+                                 long long ldh) {
+    long long total = (long long)r * m;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        long long u = k / r, a = k % r;
+        Hb[a * ldh + u] = __float2bfloat16_rn(H[k]);
+    }
+}
+
+// ------------------------------------------------------------------------
+// update kernels (FP32): the multiplicative rule of nmf_kernels.cu:43-47,
+// with the numerator summed from the GEMM's partial slots in a fixed order
+// and the denominator product (W'W H or W H H', K = r) formed here in FP32.
+// ------------------------------------------------------------------------
+constexpr int kUpdCols = 32;  // columns (H-step) or rows (W-step) per CTA
+constexpr int kUpdThreads = 256;
+
+// H(a,u) *= num(a,u) / (sum_b G(a,b) H(b,u) + eps);  also writes Hb (row-major BF16)
+__global__ void __launch_bounds__(kUpdThreads)
+    tc_update_h_kernel(float *__restrict__ H, __nv_bfloat16 *__restrict__ Hb, long long ldh,
+                       const float *__restrict__ G, const float *__restrict__ P, const int *__restrict__ slot_ptr,
+                       const int *__restrict__ slot_list, int r, int m, int npad, float eps) {
+    extern __shared__ float sm[];
+    float *Gs = sm;                          // [r][r]   G(b,a) at b*r + a (G is symmetric)
+    float *Hs = Gs + r * r;                  // [r][33]  H tile, later the new values
+    float *Ns = Hs + r * (kUpdCols + 1);     // [r][33]  numerators
+    const int u0 = blockIdx.x * kUpdCols;
+    const int tile = u0 / kTileM, lrow0 = u0 % kTileM;
+    const int ncol = min(kUpdCols, m - u0);
+    for (int k = threadIdx.x; k < r * r; k += blockDim.x) Gs[k] = G[k];
+    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x) {
+        int uc = k / r, a = k % r;
+        Hs[a * (kUpdCols + 1) + uc] = H[(long long)(u0 + uc) * r + a];
+    }
+    const int s0 = slot_ptr[tile], s1 = slot_ptr[tile + 1];
+    for (int k = threadIdx.x; k < ncol * npad; k += blockDim.x) {
+        int uc = k / npad, a = k % npad;
+        if (a >= r) continue;
+        float acc = 0.f;
+        for (int s = s0; s < s1; s++)
+            acc += P[((size_t)slot_list[s] * kTileM + lrow0 + uc) * npad + a];
+        Ns[a * (kUpdCols + 1) + uc] = acc;
+    }
+    __syncthreads();
+    float hn[(kUpdCols * kMaxRank) / kUpdThreads];
+    int cnt = 0;
+    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x, cnt++) {
+        int uc = k / r, a = k % r;
+        float den = 0.f;
+        for (int b = 0; b < r; b++) den = fmaf(Gs[b * r + a], Hs[b * (kUpdCols + 1) + uc], den);
+        float h = Hs[a * (kUpdCols + 1) + uc];
+        h *= Ns[a * (kUpdCols + 1) + uc] / (den + eps);
+        hn[cnt] = h;
+        H[(long long)(u0 + uc) * r + a] = h;
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x, cnt++) {
+        int uc = k / r, a = k % r;
+        Hs[a * (kUpdCols + 1) + uc] = hn[cnt];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x) {
+        int a = k / ncol, uc = k % ncol;
+        Hb[(long long)a * ldh + u0 + uc] = __float2bfloat16_rn(Hs[a * (kUpdCols + 1) + uc]);
+    }
+}
+
+// W(i,a) *= num(i,a) / (sum_b W(i,b) G(b,a) + eps);  also writes Wb (column-major BF16)
+__global__ void __launch_bounds__(kUpdThreads)
+    tc_update_w_kernel(float *__restrict__ W, __nv_bfloat16 *__restrict__ Wb, long long ldw,
+                       const float *__restrict__ G, const float *__restrict__ P, const int *__restrict__ slot_ptr,
+                       const int *__restrict__ slot_list, int r, int n, int npad, float eps) {
+    extern __shared__ float sm[];
+    float *Gs = sm;                          // [r][r]
+    float *Ws = Gs + r * r;                  // [r][33]  W(i,a) at a*33 + il
+    float *Ns = Ws + r * (kUpdCols + 1);     // [r][33]
+    const int i0 = blockIdx.x * kUpdCols;
+    const int tile = i0 / kTileM, lrow0 = i0 % kTileM;
+    const int nrow = min(kUpdCols, n - i0);
+    for (int k = threadIdx.x; k < r * r; k += blockDim.x) Gs[k] = G[k];
+    for (int k = threadIdx.x; k < r * kUpdCols; k += blockDim.x) {
+        int a = k / kUpdCols, il = k % kUpdCols;
+        if (il < nrow) Ws[a * (kUpdCols + 1) + il] = W[(long long)a * n + i0 + il];
+    }
+    const int s0 = slot_ptr[tile], s1 = slot_ptr[tile + 1];
+    for (int k = threadIdx.x; k < nrow * npad; k += blockDim.x) {
+        int il = k / npad, a = k % npad;
+        if (a >= r) continue;
+        float acc = 0.f;
+        for (int s = s0; s < s1; s++)
+            acc += P[((size_t)slot_list[s] * kTileM + lrow0 + il) * npad + a];
+        Ns[a * (kUpdCols + 1) + il] = acc;
+    }
+    __syncthreads();
+    float wn[(kUpdCols * kMaxRank) / kUpdThreads];
+    int cnt = 0;
+    for (int k = threadIdx.x; k < r * nrow; k += blockDim.x, cnt++) {
+        int il = k / r, a = k % r;
+        float den = 0.f;
+        for (int b = 0; b < r; b++) den = fmaf(Ws[b * (kUpdCols + 1) + il], Gs[b * r + a], den);
+        float w = Ws[a * (kUpdCols + 1) + il];
+        w *= Ns[a * (kUpdCols + 1) + il] / (den + eps);
+        wn[cnt] = w;
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int k = threadIdx.x; k < r * nrow; k += blockDim.x, cnt++) {
+        int il = k / r, a = k % r;
+        Ws[a * (kUpdCols + 1) + il] = wn[cnt];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < r * kUpdCols; k += blockDim.x) {
+        int a = k / kUpdCols, il = k % kUpdCols;
+        if (il >= nrow) continue;
+        float w = Ws[a * (kUpdCols + 1) + il];
+        W[(long long)a * n + i0 + il] = w;
+        Wb[(long long)a * ldw + i0 + il] = __float2bfloat16_rn(w);
+    }
+}
+
+// ------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------
+}  // namespace gpunmf
+
+struct TcGemm {
+    CUtensorMap tmA, tmB;
+    gpunmf::SkParams p;
+    int grid = 0;
+    int smem = 0;
+    int *slot_ptr = nullptr, *slot_list = nullptr;
+};
+
+struct TcState {
+    __nv_bfloat16 *Vb = nullptr, *Vbt = nullptr, *Wb = nullptr, *Hb = nullptr;
+    long long ldv = 0, ldvt = 0, ldw = 0, ldh = 0;
+    int npad = 16;
+    TcGemm gh, gw;  // H-step (W'V) and W-step (VH')
+    float *P_h = nullptr, *P_w = nullptr;
+    int *err = nullptr;
+    float *G_h = nullptr;  // H H'
+};
+
+namespace gpunmf {
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2-D BF16 tensor map: dim0 contiguous (extent d0), dim1 with stride ld elements; box {64, box1}, 128B swizzle
+static gpunmf_status make_map(CUtensorMap *m, const void *base, uint64_t d0, uint64_t d1, uint64_t ld,
+                              uint32_t box1) {
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return GPUNMF_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {d0, d1};
+    cuuint64_t strides[1] = {ld * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBlockK, box1};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return GPUNMF_ERR_CUDA;
+    }
+    return GPUNMF_OK;
+}
+
+static int num_sms() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            sms = kNumSMsGB300;
+    }
+    return sms;
+}
+
+// stream-K schedule: CTA c covers [c*T/G, (c+1)*T/G); its segments at tile boundaries get slots
+// c*max_seg + s.  Builds the per-tile slot lists in CTA order.
+static void schedule(int tiles, int kblocks, int G, int *max_seg, std::vector<int> &ptr, std::vector<int> &list) {
+    long long T = (long long)tiles * kblocks;
+    int ms = 1;
+    std::vector<std::vector<int>> per(tiles);
+    std::vector<std::vector<int>> segs_tile(G);
+    for (int c = 0; c < G; c++) {
+        long long lo = (long long)c * T / G, hi = (long long)(c + 1) * T / G;
+        int s = 0;
+        for (long long b = lo; b < hi;) {
+            long long t = b / kblocks, e = std::min(hi, (t + 1) * kblocks);
+            segs_tile[c].push_back((int)t);
+            s++;
+            b = e;
+        }
+        ms = std::max(ms, s);
+    }
+    for (int c = 0; c < G; c++)
+        for (size_t s = 0; s < segs_tile[c].size(); s++) per[segs_tile[c][s]].push_back(c * ms + (int)s);
+    ptr.assign(tiles + 1, 0);
+    list.clear();
+    for (int t = 0; t < tiles; t++) {
+        ptr[t] = (int)list.size();
+        for (int x : per[t]) list.push_back(x);
+    }
+    ptr[tiles] = (int)list.size();
+    *max_seg = ms;
+}
+
+static gpunmf_status setup_gemm(TcGemm &g, int rows, int K, int npad, float **partials, int *err) {
+    const int tiles = ceil_div(rows, kTileM);
+    const int kblocks = ceil_div(K, kBlockK);
+    const long long T = (long long)tiles * kblocks;
+    g.grid = (int)std::min<long long>(num_sms(), T);
+    std::vector<int> ptr, list;
+    int max_seg = 1;
+    schedule(tiles, kblocks, g.grid, &max_seg, ptr, list);
+    const int stageB = npad * kBlockK * 2;
+    int stages = std::min(kMaxStages, (kSmemBudget - 1024 - 256) / (kStageABytes + stageB));
+    g.p.tiles = tiles;
+    g.p.kblocks = kblocks;
+    g.p.npad = npad;
+    g.p.stages = stages;
+    g.p.max_seg = max_seg;
+    uint32_t cols = 32;
+    while (cols < (uint32_t)(2 * npad)) cols <<= 1;
+    g.p.tmem_cols = cols;
+    g.p.err = err;
+    g.smem = 1024 + stages * (kStageABytes + stageB) + (2 * stages + 5) * 8 + 16;
+    size_t slots = (size_t)g.grid * max_seg;
+    cudaError_t e = cudaMalloc((void **)partials, slots * kTileM * npad * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&g.slot_ptr, ptr.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&g.slot_list, std::max<size_t>(1, list.size()) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(g.slot_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !list.empty())
+        e = cudaMemcpy(g.slot_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_error("tensor-core workspace allocation failed: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return GPUNMF_ERR_NOMEM;
+    }
+    g.p.partials = *partials;
+    return GPUNMF_OK;
+}
+
+static size_t gemm_partial_bytes(int rows, int K, int npad) {
+    const int tiles = ceil_div(rows, kTileM), kblocks = ceil_div(K, kBlockK);
+    long long T = (long long)tiles * kblocks;
+    int G = (int)std::min<long long>(kNumSMsGB300, T);
+    long long per = (T + G - 1) / G;
+    long long max_seg = per / kblocks + 2;
+    return (size_t)G * max_seg * kTileM * npad * sizeof(float) + (size_t)(tiles + 1 + G * max_seg) * sizeof(int);
+}
+
+gpunmf_status tc_supported(int rule, int n, int m, int r) {
+    if (rule != GPUNMF_EUCLIDEAN) {
+        set_error("BF16 tensor-core path covers the Euclidean rule");
+        return GPUNMF_ERR_UNSUPPORTED;
+    }
+    if (r > kMaxRank) {
+        set_error("BF16 path supports r <= %d", kMaxRank);
+        return GPUNMF_ERR_UNSUPPORTED;
+    }
+    (void)n;
+    (void)m;
+    return GPUNMF_OK;
+}
+
 void tc_add_sizes(int, int, int, int, size_t *) {}
-size_t tc_footprint(int, int, int, int) { return 0; }
-gpunmf_status tc_create(gpunmf_job *) { return GPUNMF_ERR_UNSUPPORTED; }
-gpunmf_status tc_prepare(gpunmf_job *) { return GPUNMF_ERR_UNSUPPORTED; }
-gpunmf_status tc_iterate(gpunmf_job *, bool) { return GPUNMF_ERR_UNSUPPORTED; }
-void tc_destroy(gpunmf_job *) {}
+
+size_t tc_footprint(int rule, int n, int m, int r) {
+    (void)rule;
+    const int npad = npad_of(r);
+    size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r);
+    b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
+    b += (size_t)r * r * sizeof(float) + 64;
+    return b;
+}
+
+gpunmf_status tc_create(gpunmf_job *j) {
+    TcState *t = new (std::nothrow) TcState();
+    if (!t) return GPUNMF_ERR_NOMEM;
+    j->tc = t;
+    const int n = j->n, m = j->m, r = j->r;
+    t->npad = npad_of(r);
+    t->ldv = ceil8(n);
+    t->ldvt = ceil8(m);
+    t->ldw = ceil8(n);
+    t->ldh = ceil8(m);
+    cudaError_t e = cudaMalloc((void **)&t->Vb, (size_t)t->ldv * m * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->Vbt, (size_t)t->ldvt * n * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->Wb, (size_t)t->ldw * r * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->Hb, (size_t)t->ldh * r * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->G_h, (size_t)r * r * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(t->err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        set_error("tensor-core buffers: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return GPUNMF_ERR_NOMEM;
+    }
+    gpunmf_status st = setup_gemm(t->gh, m, n, t->npad, &t->P_h, t->err);
+    if (st == GPUNMF_OK) st = setup_gemm(t->gw, n, m, t->npad, &t->P_w, t->err);
+    if (st != GPUNMF_OK) return st;
+    // H-step: rows = u (columns of V): A = Vb (dim0 i over n, dim1 u over m); B = Wb (dim0 i, dim1 a)
+    st = make_map(&t->gh.tmA, t->Vb, n, m, t->ldv, kTileM);
+    if (st == GPUNMF_OK) st = make_map(&t->gh.tmB, t->Wb, n, r, t->ldw, t->npad);
+    // W-step: rows = i: A = Vbt (dim0 u over m, dim1 i over n); B = Hb (dim0 u, dim1 a)
+    if (st == GPUNMF_OK) st = make_map(&t->gw.tmA, t->Vbt, m, n, t->ldvt, kTileM);
+    if (st == GPUNMF_OK) st = make_map(&t->gw.tmB, t->Hb, m, r, t->ldh, t->npad);
+    if (st != GPUNMF_OK) return st;
+    int maxsmem = std::max(t->gh.smem, t->gw.smem);
+    e = cudaFuncSetAttribute(tc_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+    if (e == cudaSuccess) {
+        int upd = (r * r + 2 * r * (kUpdCols + 1)) * (int)sizeof(float);
+        e = cudaFuncSetAttribute(tc_update_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, upd);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tc_update_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, upd);
+    }
+    if (e != cudaSuccess) {
+        set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        return GPUNMF_ERR_CUDA;
+    }
+    return GPUNMF_OK;
+}
+
+gpunmf_status tc_prepare(gpunmf_job *j) {
+    TcState *t = j->tc;
+    cudaStream_t s = j->stream;
+    dim3 grid(ceil_div(j->n, 32), ceil_div(j->m, 32));
+    convert_v_kernel<<<grid, dim3(32, 8), 0, s>>>(j->V, j->n, j->m, t->Vb, t->ldv, t->Vbt, t->ldvt);
+    convert_w_kernel<<<std::min(1024, ceil_div((long long)j->n * j->r, 256)), 256, 0, s>>>(j->W, j->n, j->r,
+                                                                                          t->Wb, t->ldw);
+    convert_h_kernel<<<std::min(1024, ceil_div((long long)j->r * j->m, 256)), 256, 0, s>>>(j->H, j->r, j->m,
+                                                                                          t->Hb, t->ldh);
+    GPUNMF_CUDA_TRY(cudaGetLastError());
+    return GPUNMF_OK;
+}
+
+static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
+    tc_gemm_sk_kernel<<<g.grid, kGemmThreads, g.smem, s>>>(g.tmA, g.tmB, g.p);
+    return cudaGetLastError();
+}
+
+static gpunmf_status gram(gpunmf_job *j, bool of_w, float *out) {
+    const int n = j->n, m = j->m, r = j->r;
+    cudaStream_t s = j->stream;
+    int K = of_w ? n : m;
+    int sg = gemm_f32_splits(r, r, K);
+    float *dst = sg > 1 ? j->P_g : out;
+    if (of_w)
+        GPUNMF_CUDA_TRY(gemm_f32(r, r, n, {j->W, n, true}, {j->W, n, false}, dst, r, sg, s));
+    else
+        GPUNMF_CUDA_TRY(gemm_f32(r, r, m, {j->H, r, false}, {j->H, r, true}, dst, r, sg, s));
+    if (sg > 1) GPUNMF_CUDA_TRY(sum_partials(out, j->P_g, sg, (long long)r * r, s));
+    j->launches += 1 + (sg > 1);
+    return GPUNMF_OK;
+}
+
+gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
+    TcState *t = j->tc;
+    const int n = j->n, m = j->m, r = j->r;
+    cudaStream_t s = j->stream;
+    const int updsmem = (r * r + 2 * r * (kUpdCols + 1)) * (int)sizeof(float);
+    {
+        gpunmf_status st = job_quality_step(j, true);
+        if (st != GPUNMF_OK) return st;
+    }
+    // H <- H .* (W'V) ./ (W'W H + eps)
+    {
+        gpunmf_status st = gram(j, true, j->G);
+        if (st != GPUNMF_OK) return st;
+    }
+    mark_begin(j);
+    GPUNMF_CUDA_TRY(launch_gemm(t->gh, s));
+    mark_end(j);
+    tc_update_h_kernel<<<ceil_div(m, kUpdCols), kUpdThreads, updsmem, s>>>(
+        j->H, t->Hb, t->ldh, j->G, t->P_h, t->gh.slot_ptr, t->gh.slot_list, r, m, t->npad, j->eps);
+    GPUNMF_CUDA_TRY(cudaGetLastError());
+    j->launches += 2;
+    if (!updateW) return GPUNMF_OK;
+    // W <- W .* (V H') ./ (W H H' + eps)
+    {
+        gpunmf_status st = gram(j, false, t->G_h);
+        if (st != GPUNMF_OK) return st;
+    }
+    mark_begin(j);
+    GPUNMF_CUDA_TRY(launch_gemm(t->gw, s));
+    mark_end(j);
+    tc_update_w_kernel<<<ceil_div(n, kUpdCols), kUpdThreads, updsmem, s>>>(
+        j->W, t->Wb, t->ldw, t->G_h, t->P_w, t->gw.slot_ptr, t->gw.slot_list, r, n, t->npad, j->eps);
+    GPUNMF_CUDA_TRY(cudaGetLastError());
+    j->launches += 2;
+    return GPUNMF_OK;
+}
+
+gpunmf_status tc_check(gpunmf_job *j) {
+    if (!j->tc || !j->tc->err) return GPUNMF_OK;
+    int e = 0;
+    GPUNMF_CUDA_TRY(cudaMemcpy(&e, j->tc->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e != 0) {
+        set_error("tensor-core kernel gave up waiting (error bits 0x%x)", e);
+        return GPUNMF_ERR_TIMEOUT;
+    }
+    return GPUNMF_OK;
+}
+
+void tc_destroy(gpunmf_job *j) {
+    TcState *t = j->tc;
+    if (!t) return;
+    void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h,
+                    t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete t;
+    j->tc = nullptr;
+}
+
 }  // namespace gpunmf
