@@ -351,6 +351,41 @@ cudaError_t kl_update_w_ref(float *W, const float *H, const float *V, const floa
 // ------------------------------------------------------------------------
 constexpr int kEwThreads = 256;
 
+// sum_z P[z*count + k] in z order; eight independent loads in flight per step
+__device__ __forceinline__ float sum_slices(const float *__restrict__ P, int splits, long long count, long long k) {
+    float acc = P[k];
+    int z = 1;
+    for (; z + 8 <= splits; z += 8) {
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) v[q] = P[(long long)(z + q) * count + k];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc += v[q];
+    }
+    for (; z < splits; z++) acc += P[(long long)z * count + k];
+    return acc;
+}
+
+__device__ __forceinline__ float4 sum_slices4(const float4 *__restrict__ P, int splits, long long count4,
+                                              long long k) {
+    float4 acc = P[k];
+    int z = 1;
+    for (; z + 4 <= splits; z += 4) {
+        float4 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) v[q] = P[(long long)(z + q) * count4 + k];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            acc.x += v[q].x; acc.y += v[q].y; acc.z += v[q].z; acc.w += v[q].w;
+        }
+    }
+    for (; z < splits; z++) {
+        float4 q = P[(long long)z * count4 + k];
+        acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
+    }
+    return acc;
+}
+
 static int ew_blocks(long long count, int per_thread = 4) {
     long long b = (count + (long long)kEwThreads * per_thread - 1) / ((long long)kEwThreads * per_thread);
     long long cap = 8LL * kNumSMsGB300;
@@ -363,8 +398,7 @@ __global__ void euclid_update_kernel(float *__restrict__ X, const float *__restr
                                      const float *__restrict__ D, long long count, float eps) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride) {
-        float num = P[k];
-        for (int z = 1; z < splits; z++) num += P[(long long)z * count + k];
+        float num = sum_slices(P, splits, count, k);
         X[k] *= num / (D[k] + eps);
     }
 }
@@ -373,11 +407,7 @@ __global__ void euclid_update_kernel_v4(float4 *__restrict__ X, const float4 *__
                                         const float4 *__restrict__ D, long long count4, float eps) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count4; k += stride) {
-        float4 num = P[k];
-        for (int z = 1; z < splits; z++) {
-            float4 q = P[(long long)z * count4 + k];
-            num.x += q.x; num.y += q.y; num.z += q.z; num.w += q.w;
-        }
+        float4 num = sum_slices4(P, splits, count4, k);
         float4 d = D[k], x = X[k];
         x.x *= num.x / (d.x + eps);
         x.y *= num.y / (d.y + eps);
@@ -407,9 +437,7 @@ __global__ void sum_partials_kernel(float *__restrict__ out, const float *__rest
                                     long long count) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride) {
-        float acc = P[k];
-        for (int z = 1; z < splits; z++) acc += P[(long long)z * count + k];
-        out[k] = acc;
+        out[k] = sum_slices(P, splits, count, k);
     }
 }
 
@@ -424,8 +452,7 @@ __global__ void kl_update_kernel(float *__restrict__ X, const float *__restrict_
                                  long long mod) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride) {
-        float acc = P[k];
-        for (int z = 1; z < splits; z++) acc += P[(long long)z * count + k];
+        float acc = sum_slices(P, splits, count, k);
         X[k] *= (acc / sums[(k / div) % mod]);
     }
 }
@@ -442,6 +469,7 @@ __global__ void col_sums_kernel(const float *__restrict__ X, int rows, float eps
     __shared__ double red[32];
     const float *col = X + (long long)blockIdx.x * rows;
     float s = 0.f;
+#pragma unroll 8
     for (int i = threadIdx.x; i < rows; i += blockDim.x) s += col[i];
     double t = block_sum((double)s, red);
     if (threadIdx.x == 0) {
@@ -456,6 +484,7 @@ __global__ void row_sums_kernel(const float *__restrict__ H, int r, int m, float
     __shared__ double red[32];
     const int a = blockIdx.x;
     float s = 0.f;
+#pragma unroll 8
     for (int u = threadIdx.x; u < m; u += blockDim.x) s += H[(long long)u * r + a];
     double t = block_sum((double)s, red);
     if (threadIdx.x == 0) {
@@ -483,6 +512,7 @@ __global__ void quality_ew_kernel(const float *__restrict__ V, const float *__re
     __shared__ double red[32];
     double t = 0.0;
     long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 4
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride) {
         float wh = WH[k];
         t += (double)(V[k] * log10f(wh + eps) - wh);
@@ -502,6 +532,7 @@ __global__ void kl_objective_kernel(const float *__restrict__ V, const float *__
     __shared__ double red[32];
     double t = 0.0;
     long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 4
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride) {
         double v = V[k], wh = WH[k];
         t += (v > 0.0 ? v * log(v / wh) : 0.0) - v + wh;

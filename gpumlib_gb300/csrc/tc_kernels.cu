@@ -46,7 +46,7 @@ constexpr int kBlockK = 64;
 constexpr int kGemmThreads = 192;
 constexpr int kStageABytes = kTileM * kBlockK * 2;
 constexpr int kMaxStages = 8;
-constexpr int kSmemBudget = 220 * 1024;
+constexpr int kSmemBudget = 176 * 1024;  // leaves room for one update-kernel CTA beside a GEMM CTA
 constexpr int kMaxRank = 192;  // update kernels keep an r x r Gram plus two r x 33 tiles in shared memory
 
 static inline long long ceil8(long long x) { return (x + 7) / 8 * 8; }
@@ -57,6 +57,11 @@ struct SkParams {
     uint32_t tmem_cols;
     float *partials;
     int *err;
+    // Gram reduction done by the epilogue warps: gram_out[e] = sum_z gram_partials[z*E + e]
+    const float *gram_partials;
+    float *gram_out;
+    int gram_count;
+    int gram_entries;
 };
 
 extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
@@ -103,15 +108,21 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         tmem_alloc(tmem_slot, p.tmem_cols);
         tmem_relinquish();
     }
+    if (threadIdx.x == 0) {
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // everything above overlaps the previous kernel; its outputs (the B operand, the Gram
+    // partials) are read only after this point
+    griddep_wait();
+    griddep_launch_dependents();
 
     if (warp == 0) {
         if (lane == 0) {
-            tma_prefetch_desc(&tmA);
-            tma_prefetch_desc(&tmB);
             int stage = 0;
             uint32_t phase = 0;
             int armed[kMaxStages];
@@ -131,10 +142,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             if (*((volatile int *)p.err) != 0) {
                 // error exit: let the copies already issued land before the CTA leaves
                 for (int s = 0; s < p.stages; s++)
-                    if (armed[s] > 0) {
-                        int dummy = 0;
-                        mbar_wait(&full[s], (uint32_t)((armed[s] - 1) & 1), &dummy, 1);
-                    }
+                    if (armed[s] > 0) mbar_wait_quiet(&full[s], (uint32_t)((armed[s] - 1) & 1));
             }
         }
     } else if (warp == 1) {
@@ -178,10 +186,35 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             }
             // all MMAs issued by this thread have completed once mdone flips
             tc_commit(mdone);
-            int dummy = 0;
-            mbar_wait(mdone, 0, &dummy, 1);
+            mbar_wait_quiet(mdone, 0);
         }
     } else {
+        // While the first accumulator fills, finish the Gram matrix the update kernel of the
+        // previous half-step left as per-CTA partials: this CTA owns entries
+        // [c*E/G, (c+1)*E/G); four lanes share an entry and sum the partials in a fixed order.
+        if (p.gram_out) {
+            const int et = threadIdx.x - 64;  // 0..127
+            const long long E = p.gram_entries;
+            const long long e0 = (long long)blockIdx.x * E / gridDim.x, e1 = (long long)(blockIdx.x + 1) * E / gridDim.x;
+            for (long long eb = e0; eb < e1; eb += 32) {
+                const long long e = eb + (et >> 2);
+                float s = 0.f;
+                if (e < e1) {
+                    int z = et & 3;
+                    for (; z + 28 < p.gram_count; z += 32) {
+                        float v[8];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) v[q] = p.gram_partials[(size_t)(z + 4 * q) * E + e];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) s += v[q];
+                    }
+                    for (; z < p.gram_count; z += 4) s += p.gram_partials[(size_t)z * E + e];
+                }
+                s += __shfl_xor_sync(0xffffffffu, s, 1);
+                s += __shfl_xor_sync(0xffffffffu, s, 2);
+                if (e < e1 && (et & 3) == 0) p.gram_out[e] = s;
+            }
+        }
         const int quarter = warp & 3;
         const int row = quarter * 32 + lane;
         int acc = 0, seg = 0;
@@ -265,114 +298,215 @@ __global__ void convert_h_kernel(const float *__restrict__ H, int r, int m, __nv
 }
 
 // ------------------------------------------------------------------------
-// update kernels (FP32): the multiplicative rule of nmf_kernels.cu:43-47,
-// with the numerator summed from the GEMM's partial slots in a fixed order
-// and the denominator product (W'W H or W H H', K = r) formed here in FP32.
+// update kernel (FP32): the multiplicative rule of nmf_kernels.cu:43-47 on an
+// r x 32 tile X of the factor being updated, with
+//   H-step: X = H(:, u0:u0+32),   den = G_W X          (G_W = W'W)
+//   W-step: X = W(i0:i0+32, :)',  den = G_H X = (X' G_H)'  (G_H = H H', symmetric)
+// The numerator is the sum of the GEMM's partial slots for the tile (fixed
+// order).  The kernel writes X (FP32), its BF16 copy for the next GEMM, and
+// this CTA's partial Gram X X' (r x r) that the next GEMM's epilogue warps
+// reduce.  256 threads as a 16 x 16 grid; RP = r rounded up to 16, so each
+// thread owns RP/16 rows of the tile.
 // ------------------------------------------------------------------------
-constexpr int kUpdCols = 32;  // columns (H-step) or rows (W-step) per CTA
+constexpr int kUpdCols = 32;
 constexpr int kUpdThreads = 256;
+constexpr int kSlotW = 8;  // width of the per-tile slot table (tiles with more slots use the CSR lists)
 
-// H(a,u) *= num(a,u) / (sum_b G(a,b) H(b,u) + eps);  also writes Hb (row-major BF16)
-__global__ void __launch_bounds__(kUpdThreads)
-    tc_update_h_kernel(float *__restrict__ H, __nv_bfloat16 *__restrict__ Hb, long long ldh,
-                       const float *__restrict__ G, const float *__restrict__ P, const int *__restrict__ slot_ptr,
-                       const int *__restrict__ slot_list, int r, int m, int npad, float eps) {
-    extern __shared__ float sm[];
-    float *Gs = sm;                          // [r][r]   G(b,a) at b*r + a (G is symmetric)
-    float *Hs = Gs + r * r;                  // [r][33]  H tile, later the new values
-    float *Ns = Hs + r * (kUpdCols + 1);     // [r][33]  numerators
-    const int u0 = blockIdx.x * kUpdCols;
-    const int tile = u0 / kTileM, lrow0 = u0 % kTileM;
-    const int ncol = min(kUpdCols, m - u0);
-    for (int k = threadIdx.x; k < r * r; k += blockDim.x) Gs[k] = G[k];
-    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x) {
-        int uc = k / r, a = k % r;
-        Hs[a * (kUpdCols + 1) + uc] = H[(long long)(u0 + uc) * r + a];
-    }
-    const int s0 = slot_ptr[tile], s1 = slot_ptr[tile + 1];
-    for (int k = threadIdx.x; k < ncol * npad; k += blockDim.x) {
-        int uc = k / npad, a = k % npad;
-        if (a >= r) continue;
-        float acc = 0.f;
-        for (int s = s0; s < s1; s++)
-            acc += P[((size_t)slot_list[s] * kTileM + lrow0 + uc) * npad + a];
-        Ns[a * (kUpdCols + 1) + uc] = acc;
-    }
-    __syncthreads();
-    float hn[(kUpdCols * kMaxRank) / kUpdThreads];
-    int cnt = 0;
-    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x, cnt++) {
-        int uc = k / r, a = k % r;
-        float den = 0.f;
-        for (int b = 0; b < r; b++) den = fmaf(Gs[b * r + a], Hs[b * (kUpdCols + 1) + uc], den);
-        float h = Hs[a * (kUpdCols + 1) + uc];
-        h *= Ns[a * (kUpdCols + 1) + uc] / (den + eps);
-        hn[cnt] = h;
-        H[(long long)(u0 + uc) * r + a] = h;
-    }
-    __syncthreads();
-    cnt = 0;
-    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x, cnt++) {
-        int uc = k / r, a = k % r;
-        Hs[a * (kUpdCols + 1) + uc] = hn[cnt];
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < r * ncol; k += blockDim.x) {
-        int a = k / ncol, uc = k % ncol;
-        Hb[(long long)a * ldh + u0 + uc] = __float2bfloat16_rn(Hs[a * (kUpdCols + 1) + uc]);
-    }
-}
+struct UpdParams {
+    float *X;                 // FP32 factor (H column-major r x m, or W column-major n x r)
+    __nv_bfloat16 *Xb;        // BF16 copy: element (a, c) at a*ldb + c (Hb row-major / Wb column-major)
+    long long ldb;
+    long long ldx;            // n for W (W(c,a) at a*n + c); unused for H (H(a,c) at c*r + a)
+    const float *G;           // r x r Gram for the denominator
+    const float *P;           // GEMM partial slots [slot][128][npad]
+    const int *slot_ptr, *slot_list;
+    const int *tile_slots;    // [tiles][kSlotW] slot ids, -1 padded; null when a tile has more slots
+    float *gram_partials;     // [cta][RP*RP]
+    int r, cols, npad;
+    float eps;
+    int update;               // 0: only write the Gram partials of X (initialisation)
+};
 
-// W(i,a) *= num(i,a) / (sum_b W(i,b) G(b,a) + eps);  also writes Wb (column-major BF16)
-__global__ void __launch_bounds__(kUpdThreads)
-    tc_update_w_kernel(float *__restrict__ W, __nv_bfloat16 *__restrict__ Wb, long long ldw,
-                       const float *__restrict__ G, const float *__restrict__ P, const int *__restrict__ slot_ptr,
-                       const int *__restrict__ slot_list, int r, int n, int npad, float eps) {
+template <int RP, bool IS_W>
+__global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
+    constexpr int TA = RP / 16;
+    constexpr int LDX = kUpdCols + 1;
     extern __shared__ float sm[];
-    float *Gs = sm;                          // [r][r]
-    float *Ws = Gs + r * r;                  // [r][33]  W(i,a) at a*33 + il
-    float *Ns = Ws + r * (kUpdCols + 1);     // [r][33]
-    const int i0 = blockIdx.x * kUpdCols;
-    const int tile = i0 / kTileM, lrow0 = i0 % kTileM;
-    const int nrow = min(kUpdCols, n - i0);
-    for (int k = threadIdx.x; k < r * r; k += blockDim.x) Gs[k] = G[k];
-    for (int k = threadIdx.x; k < r * kUpdCols; k += blockDim.x) {
-        int a = k / kUpdCols, il = k % kUpdCols;
-        if (il < nrow) Ws[a * (kUpdCols + 1) + il] = W[(long long)a * n + i0 + il];
+    float *Gs = sm;                  // [RP][RP], zero outside r
+    float *Xs = Gs + RP * RP;        // [RP][LDX]  X(a, c)
+    float *Ns = Xs + RP * LDX;       // [RP][LDX]  numerators, later the new X as [c][RP + 4]
+    const int tid = threadIdx.x;
+    const int c0 = blockIdx.x * kUpdCols;
+    const int ncol = min(kUpdCols, p.cols - c0);
+    const int r = p.r;
+    griddep_wait();  // the GEMM's partial slots and Gram are complete
+    griddep_launch_dependents();
+    // Shared-memory fills: every thread first issues all of its loads (compile-time trip counts,
+    // fully unrolled), then stores, so the loads of a thread are in flight together.
+    // X tile (zero outside r rows / ncol columns)
+    constexpr int XL = RP * kUpdCols / kUpdThreads;
+    {
+        float xv[XL];
+#pragma unroll
+        for (int j = 0; j < XL; j++) {
+            const int k = tid + j * kUpdThreads;
+            if (IS_W) {
+                const int a = k / kUpdCols, c = k % kUpdCols;
+                xv[j] = (a < r && c < ncol) ? p.X[(long long)a * p.ldx + c0 + c] : 0.f;
+            } else {
+                const int c = k / RP, a = k % RP;
+                xv[j] = (a < r && c < ncol) ? p.X[(long long)(c0 + c) * r + a] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < XL; j++) {
+            const int k = tid + j * kUpdThreads;
+            if (IS_W) Xs[(k / kUpdCols) * LDX + k % kUpdCols] = xv[j];
+            else Xs[(k % RP) * LDX + k / RP] = xv[j];
+        }
     }
-    const int s0 = slot_ptr[tile], s1 = slot_ptr[tile + 1];
-    for (int k = threadIdx.x; k < nrow * npad; k += blockDim.x) {
-        int il = k / npad, a = k % npad;
-        if (a >= r) continue;
-        float acc = 0.f;
-        for (int s = s0; s < s1; s++)
-            acc += P[((size_t)slot_list[s] * kTileM + lrow0 + il) * npad + a];
-        Ns[a * (kUpdCols + 1) + il] = acc;
+    if (p.update) {  // G is RP x RP (zero outside r x r: the rows of X beyond r are zero)
+        constexpr int GL = RP * RP / kUpdThreads;
+        constexpr int GC = GL < 16 ? GL : 16;
+#pragma unroll 1
+        for (int j0 = 0; j0 < GL; j0 += GC) {
+            float gv[GC];
+#pragma unroll
+            for (int j = 0; j < GC; j++) gv[j] = (j0 + j < GL) ? p.G[tid + (j0 + j) * kUpdThreads] : 0.f;
+#pragma unroll
+            for (int j = 0; j < GC; j++)
+                if (j0 + j < GL) Gs[tid + (j0 + j) * kUpdThreads] = gv[j];
+        }
+    }
+    if (p.update) {
+        // numerators: the tile's partial slots summed in slot order.  With the fixed-width slot
+        // table every load of every slot is independent, so they are all in flight at once.
+        const int tile = c0 / 128, lrow0 = c0 % 128;
+        constexpr int PER = kUpdCols * RP / kUpdThreads;
+        float acc[PER];
+#pragma unroll
+        for (int j = 0; j < PER; j++) acc[j] = 0.f;
+        if (p.tile_slots) {
+            const int4 *ts = reinterpret_cast<const int4 *>(p.tile_slots + (size_t)tile * kSlotW);
+            const int4 sa = ts[0], sb = ts[1];
+            const int sl[kSlotW] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+#pragma unroll
+            for (int q = 0; q < kSlotW; q++) {
+                if (sl[q] >= 0) {
+                    const float *base = p.P + ((size_t)sl[q] * 128 + lrow0) * p.npad;
+#pragma unroll
+                    for (int j = 0; j < PER; j++) {
+                        const int k = tid + j * kUpdThreads, c = k / RP, a = k % RP;
+                        if (c < ncol) acc[j] += base[c * p.npad + a];
+                    }
+                }
+            }
+        } else {
+            const int s0 = p.slot_ptr[tile], s1 = p.slot_ptr[tile + 1];
+            for (int q = s0; q < s1; q++) {
+                const float *base = p.P + ((size_t)p.slot_list[q] * 128 + lrow0) * p.npad;
+#pragma unroll
+                for (int j = 0; j < PER; j++) {
+                    const int k = tid + j * kUpdThreads, c = k / RP, a = k % RP;
+                    if (c < ncol) acc[j] += base[c * p.npad + a];
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = tid + j * kUpdThreads, c = k / RP, a = k % RP;
+            Ns[a * LDX + c] = acc[j];
+        }
     }
     __syncthreads();
-    float wn[(kUpdCols * kMaxRank) / kUpdThreads];
-    int cnt = 0;
-    for (int k = threadIdx.x; k < r * nrow; k += blockDim.x, cnt++) {
-        int il = k / r, a = k % r;
-        float den = 0.f;
-        for (int b = 0; b < r; b++) den = fmaf(Ws[b * (kUpdCols + 1) + il], Gs[b * r + a], den);
-        float w = Ws[a * (kUpdCols + 1) + il];
-        w *= Ns[a * (kUpdCols + 1) + il] / (den + eps);
-        wn[cnt] = w;
+    const int ga = tid & 15, gc = tid >> 4;
+    float *Xn = Ns;  // reused as [c][RP + 4] once the numerators are in registers
+    constexpr int LDN = RP + 4;
+    if (p.update) {
+        // den(a, c) for a in ga*TA.., c in gc*2..gc*2+1
+        float den[TA][2];
+#pragma unroll
+        for (int i = 0; i < TA; i++) den[i][0] = den[i][1] = 0.f;
+        for (int b = 0; b < RP; b++) {
+            float x0 = Xs[b * LDX + gc * 2], x1 = Xs[b * LDX + gc * 2 + 1];
+#pragma unroll
+            for (int i = 0; i < TA; i++) {
+                float g = Gs[b * RP + ga * TA + i];
+                den[i][0] = fmaf(g, x0, den[i][0]);
+                den[i][1] = fmaf(g, x1, den[i][1]);
+            }
+        }
+        float nv[TA][2], xv[TA][2];
+#pragma unroll
+        for (int i = 0; i < TA; i++)
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                nv[i][j] = Ns[(ga * TA + i) * LDX + gc * 2 + j];
+                xv[i][j] = Xs[(ga * TA + i) * LDX + gc * 2 + j];
+            }
+        __syncthreads();  // everyone has read Ns and Xs
+#pragma unroll
+        for (int i = 0; i < TA; i++)
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                int a = ga * TA + i;
+                float x = xv[i][j];
+                if (a < r) x *= nv[i][j] / (den[i][j] + p.eps);
+                Xn[(gc * 2 + j) * LDN + a] = x;
+            }
+    } else {
+        for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {
+            int c = k / RP, a = k % RP;
+            Xn[c * LDN + a] = Xs[a * LDX + c];
+        }
     }
     __syncthreads();
-    cnt = 0;
-    for (int k = threadIdx.x; k < r * nrow; k += blockDim.x, cnt++) {
-        int il = k / r, a = k % r;
-        Ws[a * (kUpdCols + 1) + il] = wn[cnt];
+    if (p.update) {
+        if (IS_W) {
+            for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {
+                int a = k / kUpdCols, c = k % kUpdCols;
+                if (a < r && c < ncol) {
+                    float x = Xn[c * LDN + a];
+                    p.X[(long long)a * p.ldx + c0 + c] = x;
+                    p.Xb[(long long)a * p.ldb + c0 + c] = __float2bfloat16_rn(x);
+                }
+            }
+        } else {
+            for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {
+                int c = k / RP, a = k % RP;
+                if (a < r && c < ncol) p.X[(long long)(c0 + c) * r + a] = Xn[c * LDN + a];
+            }
+            for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {
+                int a = k / kUpdCols, c = k % kUpdCols;
+                if (a < r && c < ncol) p.Xb[(long long)a * p.ldb + c0 + c] = __float2bfloat16_rn(Xn[c * LDN + a]);
+            }
+        }
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < r * kUpdCols; k += blockDim.x) {
-        int a = k / kUpdCols, il = k % kUpdCols;
-        if (il >= nrow) continue;
-        float w = Ws[a * (kUpdCols + 1) + il];
-        W[(long long)a * n + i0 + il] = w;
-        Wb[(long long)a * ldw + i0 + il] = __float2bfloat16_rn(w);
+    // partial Gram of the new tile: rows ga*TA.., columns gb*TA.. (columns outside ncol are zero)
+    {
+        const int gb = tid >> 4;
+        float acc[TA][TA];
+#pragma unroll
+        for (int i = 0; i < TA; i++)
+#pragma unroll
+            for (int k = 0; k < TA; k++) acc[i][k] = 0.f;
+        for (int c = 0; c < kUpdCols; c++) {
+            float xa[TA], xb[TA];
+#pragma unroll
+            for (int i = 0; i < TA; i++) {
+                xa[i] = Xn[c * LDN + ga * TA + i];
+                xb[i] = Xn[c * LDN + gb * TA + i];
+            }
+#pragma unroll
+            for (int i = 0; i < TA; i++)
+#pragma unroll
+                for (int k = 0; k < TA; k++) acc[i][k] = fmaf(xa[i], xb[k], acc[i][k]);
+        }
+        float *out = p.gram_partials + (size_t)blockIdx.x * RP * RP;
+#pragma unroll
+        for (int i = 0; i < TA; i++)
+#pragma unroll
+            for (int k = 0; k < TA; k++) out[(ga * TA + i) * RP + gb * TA + k] = acc[i][k];
     }
 }
 
@@ -387,6 +521,7 @@ struct TcGemm {
     int grid = 0;
     int smem = 0;
     int *slot_ptr = nullptr, *slot_list = nullptr;
+    int *tile_slots = nullptr;
 };
 
 struct TcState {
@@ -396,7 +531,9 @@ struct TcState {
     TcGemm gh, gw;  // H-step (W'V) and W-step (VH')
     float *P_h = nullptr, *P_w = nullptr;
     int *err = nullptr;
-    float *G_h = nullptr;  // H H'
+    float *G_w = nullptr, *G_h = nullptr;     // W'W and H H', npad x npad
+    float *GP_w = nullptr, *GP_h = nullptr;   // per-CTA Gram partials of the update kernels
+    int gp_w_count = 0, gp_h_count = 0;
 };
 
 namespace gpunmf {
@@ -485,6 +622,15 @@ static gpunmf_status setup_gemm(TcGemm &g, int rows, int K, int npad, float **pa
     std::vector<int> ptr, list;
     int max_seg = 1;
     schedule(tiles, kblocks, g.grid, &max_seg, ptr, list);
+    bool table_ok = true;
+    for (int t = 0; t < tiles; t++)
+        if (ptr[t + 1] - ptr[t] > kSlotW) table_ok = false;
+    std::vector<int> table;
+    if (table_ok) {
+        table.assign((size_t)tiles * kSlotW, -1);
+        for (int t = 0; t < tiles; t++)
+            for (int q = ptr[t]; q < ptr[t + 1]; q++) table[(size_t)t * kSlotW + (q - ptr[t])] = list[q];
+    }
     const int stageB = npad * kBlockK * 2;
     int stages = std::min(kMaxStages, (kSmemBudget - 1024 - 256) / (kStageABytes + stageB));
     g.p.tiles = tiles;
@@ -504,6 +650,11 @@ static gpunmf_status setup_gemm(TcGemm &g, int rows, int K, int npad, float **pa
     if (e == cudaSuccess) e = cudaMemcpy(g.slot_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !list.empty())
         e = cudaMemcpy(g.slot_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && table_ok) {
+        e = cudaMalloc((void **)&g.tile_slots, table.size() * sizeof(int));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(g.tile_slots, table.data(), table.size() * sizeof(int), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) {
         set_error("tensor-core workspace allocation failed: %s", cudaGetErrorString(e));
         cudaGetLastError();
@@ -520,6 +671,77 @@ static size_t gemm_partial_bytes(int rows, int K, int npad) {
     long long per = (T + G - 1) / G;
     long long max_seg = per / kblocks + 2;
     return (size_t)G * max_seg * kTileM * npad * sizeof(float) + (size_t)(tiles + 1 + G * max_seg) * sizeof(int);
+}
+
+static int update_smem_bytes(int rp) {
+    int ns = std::max(rp * (kUpdCols + 1), kUpdCols * (rp + 4));
+    return (rp * rp + rp * (kUpdCols + 1) + ns) * (int)sizeof(float);
+}
+
+template <int RP>
+static cudaError_t set_update_smem_rp() {
+    cudaError_t e = cudaFuncSetAttribute(tc_update_kernel<RP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         update_smem_bytes(RP));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc_update_kernel<RP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 update_smem_bytes(RP));
+    return e;
+}
+
+static cudaError_t set_update_smem(int rp) {
+    switch (rp) {
+#define CASE(R) \
+    case R: return set_update_smem_rp<R>();
+        CASE(16) CASE(32) CASE(48) CASE(64) CASE(80) CASE(96) CASE(112) CASE(128) CASE(144) CASE(160) CASE(176)
+        CASE(192)
+#undef CASE
+    }
+    return cudaErrorInvalidValue;
+}
+
+static cudaError_t launch_update(const UpdParams &u, int rp, bool is_w, cudaStream_t s) {
+    const int grid = ceil_div(u.cols, kUpdCols);
+    const int smem = update_smem_bytes(rp);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kUpdThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    switch (rp) {
+#define CASE(R)                                                                          \
+    case R:                                                                              \
+        return is_w ? cudaLaunchKernelEx(&cfg, tc_update_kernel<R, true>, u)             \
+                    : cudaLaunchKernelEx(&cfg, tc_update_kernel<R, false>, u);
+        CASE(16) CASE(32) CASE(48) CASE(64) CASE(80) CASE(96) CASE(112) CASE(128) CASE(144) CASE(160) CASE(176)
+        CASE(192)
+#undef CASE
+    }
+    return cudaErrorInvalidValue;
+}
+
+static UpdParams update_params_h(gpunmf_job *j, int update) {
+    TcState *t = j->tc;
+    UpdParams u{};
+    u.X = j->H; u.Xb = t->Hb; u.ldb = t->ldh; u.ldx = 0; u.G = t->G_w; u.P = t->P_h;
+    u.slot_ptr = t->gh.slot_ptr; u.slot_list = t->gh.slot_list; u.tile_slots = t->gh.tile_slots;
+    u.gram_partials = t->GP_h;
+    u.r = j->r; u.cols = j->m; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    return u;
+}
+
+static UpdParams update_params_w(gpunmf_job *j, int update) {
+    TcState *t = j->tc;
+    UpdParams u{};
+    u.X = j->W; u.Xb = t->Wb; u.ldb = t->ldw; u.ldx = j->n; u.G = t->G_h; u.P = t->P_w;
+    u.slot_ptr = t->gw.slot_ptr; u.slot_list = t->gw.slot_list; u.tile_slots = t->gw.tile_slots;
+    u.gram_partials = t->GP_w;
+    u.r = j->r; u.cols = j->n; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    return u;
 }
 
 gpunmf_status tc_supported(int rule, int n, int m, int r) {
@@ -543,7 +765,7 @@ size_t tc_footprint(int rule, int n, int m, int r) {
     const int npad = npad_of(r);
     size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r);
     b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
-    b += (size_t)r * r * sizeof(float) + 64;
+    b += (size_t)npad * npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
     return b;
 }
 
@@ -562,7 +784,13 @@ gpunmf_status tc_create(gpunmf_job *j) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&t->Wb, (size_t)t->ldw * r * 2);
     if (e == cudaSuccess) e = cudaMalloc((void **)&t->Hb, (size_t)t->ldh * r * 2);
     if (e == cudaSuccess) e = cudaMalloc((void **)&t->err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->G_h, (size_t)r * r * sizeof(float));
+    const size_t rp2 = (size_t)t->npad * t->npad;
+    t->gp_w_count = ceil_div(n, kUpdCols);
+    t->gp_h_count = ceil_div(m, kUpdCols);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->G_w, rp2 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->G_h, rp2 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->GP_w, rp2 * t->gp_w_count * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->GP_h, rp2 * t->gp_h_count * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(t->err, 0, sizeof(int));
     if (e != cudaSuccess) {
         set_error("tensor-core buffers: %s", cudaGetErrorString(e));
@@ -572,6 +800,15 @@ gpunmf_status tc_create(gpunmf_job *j) {
     gpunmf_status st = setup_gemm(t->gh, m, n, t->npad, &t->P_h, t->err);
     if (st == GPUNMF_OK) st = setup_gemm(t->gw, n, m, t->npad, &t->P_w, t->err);
     if (st != GPUNMF_OK) return st;
+    // the H-step GEMM finishes W'W from the W-step update's partials, and vice versa
+    t->gh.p.gram_partials = t->GP_w;
+    t->gh.p.gram_out = t->G_w;
+    t->gh.p.gram_count = t->gp_w_count;
+    t->gh.p.gram_entries = (int)rp2;
+    t->gw.p.gram_partials = t->GP_h;
+    t->gw.p.gram_out = t->G_h;
+    t->gw.p.gram_count = t->gp_h_count;
+    t->gw.p.gram_entries = (int)rp2;
     // H-step: rows = u (columns of V): A = Vb (dim0 i over n, dim1 u over m); B = Wb (dim0 i, dim1 a)
     st = make_map(&t->gh.tmA, t->Vb, n, m, t->ldv, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->gh.tmB, t->Wb, n, r, t->ldw, t->npad);
@@ -581,12 +818,7 @@ gpunmf_status tc_create(gpunmf_job *j) {
     if (st != GPUNMF_OK) return st;
     int maxsmem = std::max(t->gh.smem, t->gw.smem);
     e = cudaFuncSetAttribute(tc_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    if (e == cudaSuccess) {
-        int upd = (r * r + 2 * r * (kUpdCols + 1)) * (int)sizeof(float);
-        e = cudaFuncSetAttribute(tc_update_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, upd);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tc_update_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, upd);
-    }
+    if (e == cudaSuccess) e = set_update_smem(t->npad);
     if (e != cudaSuccess) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return GPUNMF_ERR_CUDA;
@@ -604,62 +836,44 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
     convert_h_kernel<<<std::min(1024, ceil_div((long long)j->r * j->m, 256)), 256, 0, s>>>(j->H, j->r, j->m,
                                                                                           t->Hb, t->ldh);
     GPUNMF_CUDA_TRY(cudaGetLastError());
+    // Gram partials of the initial W, finished by the first H-step GEMM
+    GPUNMF_CUDA_TRY(launch_update(update_params_w(j, 0), t->npad, true, s));
     return GPUNMF_OK;
 }
 
 static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
-    tc_gemm_sk_kernel<<<g.grid, kGemmThreads, g.smem, s>>>(g.tmA, g.tmB, g.p);
-    return cudaGetLastError();
-}
-
-static gpunmf_status gram(gpunmf_job *j, bool of_w, float *out) {
-    const int n = j->n, m = j->m, r = j->r;
-    cudaStream_t s = j->stream;
-    int K = of_w ? n : m;
-    int sg = gemm_f32_splits(r, r, K);
-    float *dst = sg > 1 ? j->P_g : out;
-    if (of_w)
-        GPUNMF_CUDA_TRY(gemm_f32(r, r, n, {j->W, n, true}, {j->W, n, false}, dst, r, sg, s));
-    else
-        GPUNMF_CUDA_TRY(gemm_f32(r, r, m, {j->H, r, false}, {j->H, r, true}, dst, r, sg, s));
-    if (sg > 1) GPUNMF_CUDA_TRY(sum_partials(out, j->P_g, sg, (long long)r * r, s));
-    j->launches += 1 + (sg > 1);
-    return GPUNMF_OK;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.grid);
+    cfg.blockDim = dim3(kGemmThreads);
+    cfg.dynamicSmemBytes = g.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel, g.tmA, g.tmB, g.p);
 }
 
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
     TcState *t = j->tc;
-    const int n = j->n, m = j->m, r = j->r;
     cudaStream_t s = j->stream;
-    const int updsmem = (r * r + 2 * r * (kUpdCols + 1)) * (int)sizeof(float);
     {
         gpunmf_status st = job_quality_step(j, true);
         if (st != GPUNMF_OK) return st;
     }
-    // H <- H .* (W'V) ./ (W'W H + eps)
-    {
-        gpunmf_status st = gram(j, true, j->G);
-        if (st != GPUNMF_OK) return st;
-    }
+    // H <- H .* (W'V) ./ (W'W H + eps); the GEMM also finishes W'W
     mark_begin(j);
     GPUNMF_CUDA_TRY(launch_gemm(t->gh, s));
     mark_end(j);
-    tc_update_h_kernel<<<ceil_div(m, kUpdCols), kUpdThreads, updsmem, s>>>(
-        j->H, t->Hb, t->ldh, j->G, t->P_h, t->gh.slot_ptr, t->gh.slot_list, r, m, t->npad, j->eps);
-    GPUNMF_CUDA_TRY(cudaGetLastError());
+    GPUNMF_CUDA_TRY(launch_update(update_params_h(j, 1), t->npad, false, s));
     j->launches += 2;
     if (!updateW) return GPUNMF_OK;
-    // W <- W .* (V H') ./ (W H H' + eps)
-    {
-        gpunmf_status st = gram(j, false, t->G_h);
-        if (st != GPUNMF_OK) return st;
-    }
+    // W <- W .* (V H') ./ (W H H' + eps); the GEMM also finishes H H'
     mark_begin(j);
     GPUNMF_CUDA_TRY(launch_gemm(t->gw, s));
     mark_end(j);
-    tc_update_w_kernel<<<ceil_div(n, kUpdCols), kUpdThreads, updsmem, s>>>(
-        j->W, t->Wb, t->ldw, t->G_h, t->P_w, t->gw.slot_ptr, t->gw.slot_list, r, n, t->npad, j->eps);
-    GPUNMF_CUDA_TRY(cudaGetLastError());
+    GPUNMF_CUDA_TRY(launch_update(update_params_w(j, 1), t->npad, true, s));
     j->launches += 2;
     return GPUNMF_OK;
 }
@@ -678,8 +892,9 @@ gpunmf_status tc_check(gpunmf_job *j) {
 void tc_destroy(gpunmf_job *j) {
     TcState *t = j->tc;
     if (!t) return;
-    void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h,
-                    t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list};
+    void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h, t->G_w, t->GP_h, t->GP_w,
+                    t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list,
+                    t->gh.tile_slots, t->gw.tile_slots};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete t;
