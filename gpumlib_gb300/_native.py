@@ -34,6 +34,7 @@ SIGNATURES = [
     ("gpunmf_quality_improvement", ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     ("gpunmf_residual_fp64", ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     ("gpunmf_objective_kl_fp64", ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    ("gpunmf_residual_fp64_noalloc", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_void_p] * 5),
     ("gpunmf_get_w", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("gpunmf_get_h", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("gpunmf_get_wh", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),

@@ -124,6 +124,23 @@ gpunmf_status gpunmf_quality_improvement(gpunmf_handle h, float *out);
  * WH in FP32 from the FP32 factors, squares accumulated in FP64 on the GPU. */
 gpunmf_status gpunmf_residual_fp64(gpunmf_handle h, double *out);
 
+/*
+ * Allocation-free relative residual (no counterpart in the reference).
+ * ||V - W H||_F / ||V||_F of caller-owned DEVICE matrices (column-major FP32),
+ * computed like gpunmf_residual_fp64 and written to the DEVICE double
+ * *dResult on `stream` (NULL = legacy default stream); returns without
+ * waiting.  For callers that must not allocate device memory at this point
+ * (a process whose memory is all reserved by its own pool, or a monitor that
+ * only holds device pointers to someone else's factors): its scratch is a
+ * fixed 1 MiB array inside the library, one FP64 pair per CTA of the W*H
+ * product, at most 65536 CTAs; larger shapes are rejected with
+ * GPUNMF_ERR_INVALID.  All calls share that array: calls that overlap on the
+ * GPU race.  The first call on each device looks up the array's address;
+ * make it before any stream capture begins.
+ */
+gpunmf_status gpunmf_residual_fp64_noalloc(int n, int m, int r, const float *dV, const float *dW,
+                                           const float *dH, double *dResult, void *stream);
+
 /* Generalised KL objective sum V log(V/WH) - V + WH (FP64 on the GPU). */
 gpunmf_status gpunmf_objective_kl_fp64(gpunmf_handle h, double *out);
 
