@@ -48,6 +48,19 @@ SIGNATURES = [
     ("gpunmf_host_free", None, [ctypes.c_void_p]),
     ("gpunmf_time_iterations", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_float_p,
                                                c_float_p, c_int_p, c_int_p]),
+    # batched small factorisations
+    ("gpunmf_batch_create", ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 6 + [ctypes.c_float,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    ("gpunmf_batch_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gpunmf_batch_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("gpunmf_batch_synchronize", ctypes.c_int, [ctypes.c_void_p]),
+    ("gpunmf_batch_time", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p]),
+    ("gpunmf_batch_get", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gpunmf_batch_residuals", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("gpunmf_batch_configs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("gpunmf_batch_set_config", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    ("gpunmf_batch_commit", ctypes.c_int, [ctypes.c_void_p]),
+    ("gpunmf_batch_reset_factors", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gpumlib_cuda_nmf_multiplicative_euclidean_update_matrix", ctypes.c_int,
      [ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_w", ctypes.c_int,

@@ -183,6 +183,37 @@ gpunmf_status gpunmf_time_iterations(gpunmf_handle h, int iters, int updateW,
                                      int *kernel_launches, int *all_launches);
 
 /* ------------------------------------------------------------------ */
+/* Batched small factorisations (Euclidean rule, FP32, ranks 1..32):   */
+/* the counterpart of FacesNMF's grouped training, which runs one NMF  */
+/* object per group in turn (src/examples/FacesNMF/FacesNMFDlg.cpp:    */
+/* 582-656).  All instances run in one persistent, graph-captured      */
+/* launch; each CTA takes whole instances, largest first.              */
+/* ------------------------------------------------------------------ */
+typedef struct gpunmf_batch gpunmf_batch;
+
+/* Instances k < count: V[k] n[k] x m[k], W[k] n[k] x r[k], H[k] r[k] x m[k] (host, column-major). */
+gpunmf_status gpunmf_batch_create(int count, const int *n, const int *m, const int *r, const float *const *V,
+                                  const float *const *W, const float *const *H, float eps,
+                                  gpunmf_batch **out);
+gpunmf_status gpunmf_batch_destroy(gpunmf_batch *b);
+/* `iters` iterations of every instance; enqueued, returns without waiting. */
+gpunmf_status gpunmf_batch_run(gpunmf_batch *b, int iters);
+gpunmf_status gpunmf_batch_synchronize(gpunmf_batch *b);
+/* Device time (CUDA events) of one gpunmf_batch_run(b, iters), milliseconds. */
+gpunmf_status gpunmf_batch_time(gpunmf_batch *b, int iters, float *ms);
+/* Copy instance k's W (n x r) and/or H (r x m) to host buffers (NULL to skip). */
+gpunmf_status gpunmf_batch_get(gpunmf_batch *b, int k, float *W, float *H);
+/* Relative Frobenius residual of every instance (count doubles), FP64 on the GPU. */
+gpunmf_status gpunmf_batch_residuals(gpunmf_batch *b, double *out);
+/* Tile configurations: returns their number; ranks[c] = rank class (4, 8, 16, 32) of config c. */
+int gpunmf_batch_configs(int *ranks, int cap);
+/* Choose instance k's tile configuration (same rank class), then commit before running. */
+gpunmf_status gpunmf_batch_set_config(gpunmf_batch *b, int k, int cfg);
+gpunmf_status gpunmf_batch_commit(gpunmf_batch *b);
+/* Overwrite every instance's W and H from host buffers (same shapes as at creation). */
+gpunmf_status gpunmf_batch_reset_factors(gpunmf_batch *b, const float *const *W, const float *const *H);
+
+/* ------------------------------------------------------------------ */
 /* Kernel API: same names and arguments as src/cuda/nmf/nmf_kernels.h. */
 /* gridDim/blockDim are accepted for source compatibility; the GB300   */
 /* kernels pick their own launch shape (vectorised, grid-stride).      */
