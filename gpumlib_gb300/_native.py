@@ -61,6 +61,21 @@ SIGNATURES = [
     ("gpunmf_batch_set_config", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     ("gpunmf_batch_commit", ctypes.c_int, [ctypes.c_void_p]),
     ("gpunmf_batch_reset_factors", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    # serving
+    ("gpunmf_server_create", ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_void_p)]),
+    ("gpunmf_server_submit", ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong] + [ctypes.c_int] * 4 +
+     [ctypes.c_ulonglong, ctypes.c_float]),
+    ("gpunmf_server_poll", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("gpunmf_server_fetch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    ("gpunmf_server_drain", ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    ("gpunmf_server_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                           ctypes.POINTER(ctypes.c_longlong), c_int_p, c_int_p,
+                                           ctypes.POINTER(ctypes.c_size_t)]),
+    ("gpunmf_server_clock", ctypes.c_double, [ctypes.c_void_p]),
+    ("gpunmf_server_destroy", ctypes.c_int, [ctypes.c_void_p]),
     ("gpumlib_cuda_nmf_multiplicative_euclidean_update_matrix", ctypes.c_int,
      [ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_w", ctypes.c_int,

@@ -56,14 +56,34 @@ static gpunmf_status check_device() {
     return GPUNMF_OK;
 }
 
+cudaError_t job_dev_alloc(gpunmf_job *j, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    return j->async_alloc ? cudaMallocAsync(p, bytes, j->stream) : cudaMalloc(p, bytes);
+}
+
+void job_dev_free(gpunmf_job *j, void *p) {
+    if (!p) return;
+    if (j->async_alloc)
+        cudaFreeAsync(p, j->stream);
+    else
+        cudaFree(p);
+}
+
+cudaError_t job_h2d(gpunmf_job *j, void *dst, const void *src, size_t bytes) {
+    if (bytes == 0) return cudaSuccess;
+    return j->async_alloc ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, j->stream)
+                          : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+}
+
 template <class T>
-static gpunmf_status dalloc(T **p, size_t count) {
+static gpunmf_status dalloc(gpunmf_job *j, T **p, size_t count) {
     *p = nullptr;
     if (count == 0) return GPUNMF_OK;
-    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    cudaError_t e = job_dev_alloc(j, (void **)p, count * sizeof(T));
     if (e != cudaSuccess) {
         *p = nullptr;
-        set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+        set_error("device allocation of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
         cudaGetLastError();
         return GPUNMF_ERR_NOMEM;
     }
@@ -113,11 +133,10 @@ static void job_free(gpunmf_job *j) {
     if (!j) return;
     if (j->tc) tc_destroy(j);
     float *fl[] = {j->V, j->W, j->H, j->P_h, j->P_w, j->P_g, j->G, j->D_h, j->D_w, j->WH, j->sums, j->d_quality};
-    for (float *p : fl)
-        if (p) cudaFree(p);
-    if (j->red) cudaFree(j->red);
-    if (j->d_scalar) cudaFree(j->d_scalar);
-    if (j->h_pinned) cudaFreeHost(j->h_pinned);
+    for (float *p : fl) job_dev_free(j, p);
+    job_dev_free(j, j->red);
+    job_dev_free(j, j->d_scalar);
+    if (j->h_pinned && !j->external_pinned) cudaFreeHost(j->h_pinned);
     if (j->qev) cudaEventDestroy(j->qev);
     for (cudaEvent_t e : j->tev) cudaEventDestroy(e);
     if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
@@ -125,7 +144,7 @@ static void job_free(gpunmf_job *j) {
 }
 
 static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int precision, void *stream,
-                               gpunmf_job **out) {
+                               gpunmf_job **out, unsigned char *pinned64 = nullptr, bool async_alloc = false) {
     *out = nullptr;
     if (rule != GPUNMF_EUCLIDEAN && rule != GPUNMF_DIVERGENCE) {
         set_error("unknown rule %d", rule);
@@ -158,6 +177,7 @@ static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int pre
         return GPUNMF_ERR_NOMEM;
     }
     j->rule = rule; j->n = n; j->m = m; j->r = r; j->eps = eps; j->precision = precision;
+    j->async_alloc = async_alloc && stream != nullptr;
     if (stream) {
         j->stream = (cudaStream_t)stream;
         j->own_stream = false;
@@ -174,7 +194,7 @@ static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int pre
     j->s_h = z.s_h; j->s_w = z.s_w; j->s_g = z.s_g;
     gpunmf_status st = GPUNMF_OK;
 #define ALLOC(ptr, cnt) \
-    if (st == GPUNMF_OK) st = dalloc(&(ptr), (cnt));
+    if (st == GPUNMF_OK) st = dalloc(j, &(ptr), (cnt));
     ALLOC(j->V, (size_t)n * m);
     ALLOC(j->W, (size_t)n * r);
     ALLOC(j->H, (size_t)r * m);
@@ -191,7 +211,11 @@ static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int pre
     ALLOC(j->d_scalar, 4);
 #undef ALLOC
     j->red_cap = z.red;
-    if (st == GPUNMF_OK) {
+    if (st == GPUNMF_OK && pinned64) {
+        j->h_pinned = pinned64;
+        j->external_pinned = true;
+        memset(j->h_pinned, 0, 64);
+    } else if (st == GPUNMF_OK) {
         cudaError_t e = cudaHostAlloc((void **)&j->h_pinned, 64, cudaHostAllocDefault);
         if (e != cudaSuccess) {
             set_error("cudaHostAlloc failed: %s", cudaGetErrorString(e));
@@ -357,10 +381,24 @@ static gpunmf_status job_iterate(gpunmf_job *j, int iters, bool updateW) {
 gpunmf_status job_quality_step(gpunmf_job *j, bool fused_wh) { return quality_step(j, fused_wh); }
 
 static gpunmf_status ensure_wh(gpunmf_job *j) {
-    if (!j->WH) TRY_STATUS(dalloc(&j->WH, (size_t)j->n * j->m));
+    if (!j->WH) TRY_STATUS(dalloc(j, &j->WH, (size_t)j->n * j->m));
     GPUNMF_CUDA_TRY(gemm_f32(j->n, j->m, j->r, {j->W, j->n, false}, {j->H, j->r, false}, j->WH, j->n, 1, j->stream));
     return GPUNMF_OK;
 }
+
+gpunmf_status job_create_empty(int rule, int n, int m, int r, float eps, int precision, cudaStream_t stream,
+                               unsigned char *pinned64, bool async_alloc, gpunmf_job **out) {
+    return job_alloc(rule, n, m, r, eps, precision, (void *)stream, out, pinned64, async_alloc);
+}
+
+gpunmf_status job_prepare(gpunmf_job *j) {
+    if (j->precision == GPUNMF_BF16) return tc_prepare(j);
+    return GPUNMF_OK;
+}
+
+gpunmf_status job_run(gpunmf_job *j, int iters, bool updateW) { return job_iterate(j, iters, updateW); }
+
+void job_release(gpunmf_job *j) { job_free(j); }
 
 }  // namespace gpunmf
 

@@ -48,9 +48,25 @@ struct gpunmf_job {
     std::vector<cudaEvent_t> tev;
 
     TcState *tc = nullptr;
+
+    // allocation mode: jobs made by the server use the stream-ordered allocator on their
+    // stream (no device-wide synchronisation on free) and a pinned block owned by the server
+    bool async_alloc = false;
+    bool external_pinned = false;
 };
 
 namespace gpunmf {
+// device memory of a job: cudaMalloc / cudaFree, or cudaMallocAsync / cudaFreeAsync on the job's stream
+cudaError_t job_dev_alloc(gpunmf_job *j, void **p, size_t bytes);
+void job_dev_free(gpunmf_job *j, void *p);
+// host -> device copy of set-up data (synchronous, or ordered on the job's stream)
+cudaError_t job_h2d(gpunmf_job *j, void *dst, const void *src, size_t bytes);
+// a job without data (the caller fills V, W, H on the job's stream, then calls job_prepare)
+gpunmf_status job_create_empty(int rule, int n, int m, int r, float eps, int precision, cudaStream_t stream,
+                               unsigned char *pinned64, bool async_alloc, gpunmf_job **out);
+gpunmf_status job_prepare(gpunmf_job *j);
+gpunmf_status job_run(gpunmf_job *j, int iters, bool updateW);
+void job_release(gpunmf_job *j);  // frees without synchronising (stream-ordered when async_alloc)
 void mark_begin(gpunmf_job *j);
 void mark_end(gpunmf_job *j);
 gpunmf_status job_quality_step(gpunmf_job *j, bool fused_wh);

@@ -31,6 +31,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -614,7 +615,7 @@ static void schedule(int tiles, int kblocks, int G, int *max_seg, std::vector<in
     *max_seg = ms;
 }
 
-static gpunmf_status setup_gemm(TcGemm &g, int rows, int K, int npad, float **partials, int *err) {
+static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int npad, float **partials, int *err) {
     const int tiles = ceil_div(rows, kTileM);
     const int kblocks = ceil_div(K, kBlockK);
     const long long T = (long long)tiles * kblocks;
@@ -644,16 +645,14 @@ static gpunmf_status setup_gemm(TcGemm &g, int rows, int K, int npad, float **pa
     g.p.err = err;
     g.smem = 1024 + stages * (kStageABytes + stageB) + (2 * stages + 5) * 8 + 16;
     size_t slots = (size_t)g.grid * max_seg;
-    cudaError_t e = cudaMalloc((void **)partials, slots * kTileM * npad * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&g.slot_ptr, ptr.size() * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&g.slot_list, std::max<size_t>(1, list.size()) * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemcpy(g.slot_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !list.empty())
-        e = cudaMemcpy(g.slot_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_ptr, ptr.size() * sizeof(int));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_list, std::max<size_t>(1, list.size()) * sizeof(int));
+    if (e == cudaSuccess) e = job_h2d(j, g.slot_ptr, ptr.data(), ptr.size() * sizeof(int));
+    if (e == cudaSuccess && !list.empty()) e = job_h2d(j, g.slot_list, list.data(), list.size() * sizeof(int));
     if (e == cudaSuccess && table_ok) {
-        e = cudaMalloc((void **)&g.tile_slots, table.size() * sizeof(int));
-        if (e == cudaSuccess)
-            e = cudaMemcpy(g.tile_slots, table.data(), table.size() * sizeof(int), cudaMemcpyHostToDevice);
+        e = job_dev_alloc(j, (void **)&g.tile_slots, table.size() * sizeof(int));
+        if (e == cudaSuccess) e = job_h2d(j, g.tile_slots, table.data(), table.size() * sizeof(int));
     }
     if (e != cudaSuccess) {
         set_error("tensor-core workspace allocation failed: %s", cudaGetErrorString(e));
@@ -671,6 +670,19 @@ static size_t gemm_partial_bytes(int rows, int K, int npad) {
     long long per = (T + G - 1) / G;
     long long max_seg = per / kblocks + 2;
     return (size_t)G * max_seg * kTileM * npad * sizeof(float) + (size_t)(tiles + 1 + G * max_seg) * sizeof(int);
+}
+
+static cudaError_t set_gemm_smem_once() {
+    static std::once_flag once;
+    static cudaError_t result = cudaSuccess;
+    std::call_once(once, [] {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        result = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (result == cudaSuccess)
+            result = cudaFuncSetAttribute(tc_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    });
+    return result;
 }
 
 static int update_smem_bytes(int rp) {
@@ -779,26 +791,26 @@ gpunmf_status tc_create(gpunmf_job *j) {
     t->ldvt = ceil8(m);
     t->ldw = ceil8(n);
     t->ldh = ceil8(m);
-    cudaError_t e = cudaMalloc((void **)&t->Vb, (size_t)t->ldv * m * 2);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->Vbt, (size_t)t->ldvt * n * 2);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->Wb, (size_t)t->ldw * r * 2);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->Hb, (size_t)t->ldh * r * 2);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->err, sizeof(int));
+    cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->ldv * m * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->ldvt * n * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hb, (size_t)t->ldh * r * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->err, sizeof(int));
     const size_t rp2 = (size_t)t->npad * t->npad;
     t->gp_w_count = ceil_div(n, kUpdCols);
     t->gp_h_count = ceil_div(m, kUpdCols);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->G_w, rp2 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->G_h, rp2 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->GP_w, rp2 * t->gp_w_count * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->GP_h, rp2 * t->gp_h_count * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemset(t->err, 0, sizeof(int));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->G_w, rp2 * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->G_h, rp2 * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->GP_w, rp2 * t->gp_w_count * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->GP_h, rp2 * t->gp_h_count * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemsetAsync(t->err, 0, sizeof(int), j->stream);
     if (e != cudaSuccess) {
         set_error("tensor-core buffers: %s", cudaGetErrorString(e));
         cudaGetLastError();
         return GPUNMF_ERR_NOMEM;
     }
-    gpunmf_status st = setup_gemm(t->gh, m, n, t->npad, &t->P_h, t->err);
-    if (st == GPUNMF_OK) st = setup_gemm(t->gw, n, m, t->npad, &t->P_w, t->err);
+    gpunmf_status st = setup_gemm(j, t->gh, m, n, t->npad, &t->P_h, t->err);
+    if (st == GPUNMF_OK) st = setup_gemm(j, t->gw, n, m, t->npad, &t->P_w, t->err);
     if (st != GPUNMF_OK) return st;
     // the H-step GEMM finishes W'W from the W-step update's partials, and vice versa
     t->gh.p.gram_partials = t->GP_w;
@@ -816,8 +828,9 @@ gpunmf_status tc_create(gpunmf_job *j) {
     if (st == GPUNMF_OK) st = make_map(&t->gw.tmA, t->Vbt, m, n, t->ldvt, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->gw.tmB, t->Hb, m, r, t->ldh, t->npad);
     if (st != GPUNMF_OK) return st;
-    int maxsmem = std::max(t->gh.smem, t->gw.smem);
-    e = cudaFuncSetAttribute(tc_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+    // The attribute is per function, shared by every job in the process: set it once to the
+    // device's opt-in maximum, never to one job's size (a concurrent job may need more).
+    e = set_gemm_smem_once();
     if (e == cudaSuccess) e = set_update_smem(t->npad);
     if (e != cudaSuccess) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
@@ -895,8 +908,7 @@ void tc_destroy(gpunmf_job *j) {
     void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h, t->G_w, t->GP_h, t->GP_w,
                     t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list,
                     t->gh.tile_slots, t->gw.tile_slots};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    for (void *p : ptrs) job_dev_free(j, p);
     delete t;
     j->tc = nullptr;
 }

@@ -214,6 +214,41 @@ gpunmf_status gpunmf_batch_commit(gpunmf_batch *b);
 gpunmf_status gpunmf_batch_reset_factors(gpunmf_batch *b, const float *const *W, const float *const *H);
 
 /* ------------------------------------------------------------------ */
+/* Serving with continuous batching.  Jobs arrive at any time; a       */
+/* scheduler thread admits each one as soon as one of `slots` stream   */
+/* slots is free and its device footprint fits `hbm_budget_bytes`,     */
+/* advances every admitted job in chunks of `check_every` iterations,  */
+/* each followed by an FP64 relative-residual check, and retires a job */
+/* at residual <= tol or max_iters iterations.  Admitted jobs' kernels  */
+/* overlap on the device.  Job data (V = A B + |N(0,0.01)|, W, H) is    */
+/* generated on the device from the job's seed.                        */
+/* ------------------------------------------------------------------ */
+typedef struct gpunmf_server gpunmf_server;
+
+typedef struct {
+    long long id;
+    int rule, n, m, r, iters, precision, status;   /* status: gpunmf_status of the job */
+    double residual, t_submit, t_admit, t_done;     /* seconds on the server clock */
+} gpunmf_server_result;
+
+/* keep_factors != 0 keeps each finished job's W and H on the host for gpunmf_server_fetch
+ * (then gpunmf_server_poll returns nothing). */
+gpunmf_status gpunmf_server_create(int slots, size_t hbm_budget_bytes, int precision, int check_every,
+                                   double tol, int max_iters, int keep_factors, gpunmf_server **out);
+gpunmf_status gpunmf_server_submit(gpunmf_server *s, long long id, int rule, int n, int m, int r,
+                                   unsigned long long seed, float eps);
+/* Move up to `cap` finished results into out[]; returns their number. */
+int gpunmf_server_poll(gpunmf_server *s, gpunmf_server_result *out, int cap);
+gpunmf_status gpunmf_server_fetch(gpunmf_server *s, long long id, gpunmf_server_result *res, float *W, float *H);
+/* Wait for every submitted job (GPUNMF_ERR_TIMEOUT after timeout_s seconds). */
+gpunmf_status gpunmf_server_drain(gpunmf_server *s, double timeout_s);
+gpunmf_status gpunmf_server_stats(gpunmf_server *s, long long *submitted, long long *finished, int *pending,
+                                  int *active, size_t *bytes_in_use);
+double gpunmf_server_clock(gpunmf_server *s);
+/* Cancels pending jobs, finishes admitted ones, frees everything. */
+gpunmf_status gpunmf_server_destroy(gpunmf_server *s);
+
+/* ------------------------------------------------------------------ */
 /* Kernel API: same names and arguments as src/cuda/nmf/nmf_kernels.h. */
 /* gridDim/blockDim are accepted for source compatibility; the GB300   */
 /* kernels pick their own launch shape (vectorised, grid-stride).      */
