@@ -47,7 +47,7 @@ constexpr int kBlockK = 64;
 constexpr int kGemmThreads = 192;
 constexpr int kStageABytes = kTileM * kBlockK * 2;
 constexpr int kMaxStages = 8;
-constexpr int kSmemBudget = 176 * 1024;  // leaves room for one update-kernel CTA beside a GEMM CTA
+constexpr int kSmemBudget = 196 * 1024;  // leaves room for one update-kernel CTA beside a GEMM CTA
 constexpr int kMaxRank = 192;  // update kernels keep an r x r Gram plus two r x 33 tiles in shared memory
 
 static inline long long ceil8(long long x) { return (x + 7) / 8 * 8; }
@@ -55,6 +55,7 @@ static inline int npad_of(int r) { return (r + 15) / 16 * 16; }
 
 struct SkParams {
     int tiles, kblocks, npad, stages, max_seg;
+    int bps;  // 64-wide TMA boxes per stage along K (1 or 2): a stage block covers bps*64 of K
     uint32_t tmem_cols;
     float *partials;
     int *err;
@@ -78,9 +79,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       SkParams p) {
     const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
-    const int stageB = p.npad * kBlockK * 2;
+    const int boxB = p.npad * kBlockK * 2;          // one 64-wide B box
+    const int stageA = kStageABytes * p.bps, stageB = boxB * p.bps;
     unsigned char *sA = reinterpret_cast<unsigned char *>(base);
-    unsigned char *sB = sA + p.stages * kStageABytes;
+    unsigned char *sB = sA + p.stages * stageA;
     uint64_t *full = reinterpret_cast<uint64_t *>(sB + p.stages * stageB);
     uint64_t *empty = full + p.stages;
     uint64_t *tfull = empty + p.stages;  // [2]
@@ -131,9 +133,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             for (long long b = lo; b < hi; b++) {
                 const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
                 if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty)) break;
-                mbar_arrive_expect_tx(&full[stage], kStageABytes + stageB);
-                tma_load_2d(sA + stage * kStageABytes, &tmA, kb * kBlockK, t * kTileM, &full[stage]);
-                tma_load_2d(sB + stage * stageB, &tmB, kb * kBlockK, 0, &full[stage]);
+                mbar_arrive_expect_tx(&full[stage], stageA + stageB);
+                // adjacent boxes along K: each row's bytes of the stage are requested back to back
+                for (int q = 0; q < p.bps; q++)
+                    tma_load_2d(sA + stage * stageA + q * kStageABytes, &tmA, (kb * p.bps + q) * kBlockK,
+                                t * kTileM, &full[stage]);
+                for (int q = 0; q < p.bps; q++)
+                    tma_load_2d(sB + stage * stageB + q * boxB, &tmB, (kb * p.bps + q) * kBlockK, 0, &full[stage]);
                 armed[stage]++;
                 if (++stage == p.stages) {
                     stage = 0;
@@ -164,12 +170,14 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + stage * kStageABytes);
-                    const uint32_t b0 = smem_u32(sB + stage * stageB);
+                    for (int q = 0; q < p.bps; q++) {
+                        const uint32_t a0 = smem_u32(sA + stage * stageA + q * kStageABytes);
+                        const uint32_t b0 = smem_u32(sB + stage * stageB + q * boxB);
 #pragma unroll
-                    for (int k = 0; k < kBlockK / 16; k++) {
-                        tc_mma_f16(d, smem_desc(a0 + k * 32, 16, 1024, 2), smem_desc(b0 + k * 32, 16, 1024, 2),
-                                   idesc, (bb > b || k > 0) ? 1u : 0u);
+                        for (int k = 0; k < kBlockK / 16; k++) {
+                            tc_mma_f16(d, smem_desc(a0 + k * 32, 16, 1024, 2), smem_desc(b0 + k * 32, 16, 1024, 2),
+                                       idesc, (bb > b || q > 0 || k > 0) ? 1u : 0u);
+                        }
                     }
                     tc_commit(&empty[stage]);
                     if (++stage == p.stages) {
@@ -309,7 +317,7 @@ __global__ void convert_h_kernel(const float *__restrict__ H, int r, int m, __nv
 // reduce.  256 threads as a 16 x 16 grid; RP = r rounded up to 16, so each
 // thread owns RP/16 rows of the tile.
 // ------------------------------------------------------------------------
-constexpr int kUpdCols = 32;
+constexpr int kUpdCols = 16;  // columns (H-step) or rows (W-step) per CTA; 16 x 16 threads
 constexpr int kUpdThreads = 256;
 constexpr int kSlotW = 8;  // width of the per-tile slot table (tiles with more slots use the CSR lists)
 
@@ -421,39 +429,44 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
     }
     __syncthreads();
     const int ga = tid & 15, gc = tid >> 4;
+    constexpr int CPT = kUpdCols / 16;  // columns per thread
     float *Xn = Ns;  // reused as [c][RP + 4] once the numerators are in registers
     constexpr int LDN = RP + 4;
     if (p.update) {
-        // den(a, c) for a in ga*TA.., c in gc*2..gc*2+1
-        float den[TA][2];
-#pragma unroll
-        for (int i = 0; i < TA; i++) den[i][0] = den[i][1] = 0.f;
-        for (int b = 0; b < RP; b++) {
-            float x0 = Xs[b * LDX + gc * 2], x1 = Xs[b * LDX + gc * 2 + 1];
-#pragma unroll
-            for (int i = 0; i < TA; i++) {
-                float g = Gs[b * RP + ga * TA + i];
-                den[i][0] = fmaf(g, x0, den[i][0]);
-                den[i][1] = fmaf(g, x1, den[i][1]);
-            }
-        }
-        float nv[TA][2], xv[TA][2];
+        // den(a, c) for a in ga*TA.., c in gc*CPT..
+        float den[TA][CPT];
 #pragma unroll
         for (int i = 0; i < TA; i++)
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                nv[i][j] = Ns[(ga * TA + i) * LDX + gc * 2 + j];
-                xv[i][j] = Xs[(ga * TA + i) * LDX + gc * 2 + j];
+            for (int j = 0; j < CPT; j++) den[i][j] = 0.f;
+        for (int b = 0; b < RP; b++) {
+            float xb[CPT];
+#pragma unroll
+            for (int j = 0; j < CPT; j++) xb[j] = Xs[b * LDX + gc * CPT + j];
+#pragma unroll
+            for (int i = 0; i < TA; i++) {
+                float g = Gs[b * RP + ga * TA + i];
+#pragma unroll
+                for (int j = 0; j < CPT; j++) den[i][j] = fmaf(g, xb[j], den[i][j]);
+            }
+        }
+        float nv[TA][CPT], xv[TA][CPT];
+#pragma unroll
+        for (int i = 0; i < TA; i++)
+#pragma unroll
+            for (int j = 0; j < CPT; j++) {
+                nv[i][j] = Ns[(ga * TA + i) * LDX + gc * CPT + j];
+                xv[i][j] = Xs[(ga * TA + i) * LDX + gc * CPT + j];
             }
         __syncthreads();  // everyone has read Ns and Xs
 #pragma unroll
         for (int i = 0; i < TA; i++)
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
+            for (int j = 0; j < CPT; j++) {
                 int a = ga * TA + i;
                 float x = xv[i][j];
                 if (a < r) x *= nv[i][j] / (den[i][j] + p.eps);
-                Xn[(gc * 2 + j) * LDN + a] = x;
+                Xn[(gc * CPT + j) * LDN + a] = x;
             }
     } else {
         for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {
@@ -617,7 +630,10 @@ static void schedule(int tiles, int kblocks, int G, int *max_seg, std::vector<in
 
 static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int npad, float **partials, int *err) {
     const int tiles = ceil_div(rows, kTileM);
-    const int kblocks = ceil_div(K, kBlockK);
+    const int boxB = npad * kBlockK * 2;
+    // two 64-wide boxes per stage when at least three such stages fit, else one
+    const int bps = (kSmemBudget - 1280) / (2 * (kStageABytes + boxB)) >= 3 ? 2 : 1;
+    const int kblocks = ceil_div(K, kBlockK * bps);
     const long long T = (long long)tiles * kblocks;
     g.grid = (int)std::min<long long>(num_sms(), T);
     std::vector<int> ptr, list;
@@ -632,8 +648,9 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
         for (int t = 0; t < tiles; t++)
             for (int q = ptr[t]; q < ptr[t + 1]; q++) table[(size_t)t * kSlotW + (q - ptr[t])] = list[q];
     }
-    const int stageB = npad * kBlockK * 2;
-    int stages = std::min(kMaxStages, (kSmemBudget - 1024 - 256) / (kStageABytes + stageB));
+    const int stage_bytes = bps * (kStageABytes + boxB);
+    int stages = std::min(kMaxStages, (kSmemBudget - 1024 - 256) / stage_bytes);
+    g.p.bps = bps;
     g.p.tiles = tiles;
     g.p.kblocks = kblocks;
     g.p.npad = npad;
@@ -643,7 +660,7 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     while (cols < (uint32_t)(2 * npad)) cols <<= 1;
     g.p.tmem_cols = cols;
     g.p.err = err;
-    g.smem = 1024 + stages * (kStageABytes + stageB) + (2 * stages + 5) * 8 + 16;
+    g.smem = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16;
     size_t slots = (size_t)g.grid * max_seg;
     cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_ptr, ptr.size() * sizeof(int));
