@@ -45,9 +45,10 @@ FALLBACK_BF16_TFLOPS = 1900.0
 
 METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
 
-# DRAM bytes per launch of the dominant kernel from the committed ncu capture
-# (profiles/ncu_<kernel>_*.txt); None until a capture of that kernel exists.
-NCU_TRAFFIC_PER_LAUNCH = {"bf16": None, "fp32": None}
+# DRAM bytes (read + write) per launch of the dominant kernel, from the committed ncu
+# captures of this workload (one --set full capture per precision, see the profiles
+# directory): tc_gemm_sk_kernel 143.77 MB + 3.27 MB; gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
+NCU_TRAFFIC_PER_LAUNCH = {"bf16": 147.04e6, "fp32": 276.09e6}
 
 
 def parse():
