@@ -527,6 +527,423 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
 // ------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------
+// ========================================================================
+// KL rule (nmf_multiplicative_divergence.cpp:29-50, nmf_kernels.cu:247-341):
+// fused  S = (W H) block -> R = V / (S + eps) -> numerator += R x factor,
+// never materialising W H.  Per 128-row output tile and 64-wide K block:
+//   MMA1  D1[128 x 64]  = A1[128 x r] B1[64 x r]^T     (S for the block, in TMEM)
+//   epilogue warps: R = V / (D1 + eps) -> BF16, written 128B-swizzled into
+//                   shared memory as the next MMA's A operand
+//   MMA2  D2[128 x N]  += R[128 x 64] B2[N x 64]^T     (numerator, in TMEM)
+//   H-step: rows u; A1 = Hc (H, column-major BF16), B1 = Wr (W, row-major),
+//           V tile from Vb, B2 = Wb;                 K = i (rows of V)
+//   W-step: rows i; A1 = Wr, B1 = Hc, V tile from Vbt, B2 = Hb;  K = u
+// MMA1 of block g+1 is issued before MMA2 of block g so the tensor core
+// works while the epilogue warps form R.  Stream-K partition and partial
+// slots as in the Euclidean GEMM; the epilogue warps also finish the
+// column/row sums (the KL denominators) from the update kernel's partials.
+// ========================================================================
+struct KlParams {
+    int tiles, kblocks, npad, stages, max_seg, nbox;
+    uint32_t tmem_cols;
+    float eps;
+    float *partials;
+    int *err;
+    const float *sum_partials;  // [count][npad] partial sums of the other factor
+    float *sum_out;             // [npad]
+    int sum_count;
+};
+
+__device__ __forceinline__ uint32_t sw128(int row, int chunk) {
+    return (uint32_t)(row * 128 + ((chunk ^ (row & 7)) << 4));
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    tc_kl_gemm_kernel(const __grid_constant__ CUtensorMap tmV, const __grid_constant__ CUtensorMap tmA1,
+                      const __grid_constant__ CUtensorMap tmB1, const __grid_constant__ CUtensorMap tmB2,
+                      KlParams p) {
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
+    const int b1Bytes = p.nbox * 8192, b2Bytes = p.npad * 128;
+    const int stageBytes = 16384 + b1Bytes + b2Bytes;
+    unsigned char *sStage = reinterpret_cast<unsigned char *>(base);
+    unsigned char *sA1 = sStage + p.stages * stageBytes;
+    unsigned char *sR = sA1 + p.nbox * 16384;  // [2][16 KB]
+    uint64_t *full = reinterpret_cast<uint64_t *>(sR + 2 * 16384);
+    uint64_t *empty = full + p.stages;
+    uint64_t *a1full = empty + p.stages, *a1empty = a1full + 1;
+    uint64_t *d1full = a1empty + 1, *d1empty = d1full + 2;
+    uint64_t *rfull = d1empty + 2, *rempty = rfull + 2;
+    uint64_t *tfull = rempty + 2, *tempty = tfull + 2;
+    uint64_t *mdone = tempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long T = (long long)p.tiles * p.kblocks;
+    const long long lo = (long long)blockIdx.x * T / gridDim.x;
+    const long long hi = (long long)(blockIdx.x + 1) * T / gridDim.x;
+    auto sV = [&](int st) { return sStage + st * stageBytes; };
+    auto sB1 = [&](int st) { return sStage + st * stageBytes + 16384; };
+    auto sB2 = [&](int st) { return sStage + st * stageBytes + 16384 + b1Bytes; };
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < p.stages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(a1full, 1);
+        mbar_init(a1empty, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&d1full[b], 1);
+            mbar_init(&d1empty[b], 4);
+            mbar_init(&rfull[b], 4);
+            mbar_init(&rempty[b], 1);
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 4);
+        }
+        mbar_init(mdone, 1);
+        fence_mbar_init();
+        tma_prefetch_desc(&tmV);
+        tma_prefetch_desc(&tmA1);
+        tma_prefetch_desc(&tmB1);
+        tma_prefetch_desc(&tmB2);
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, p.tmem_cols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tD1 = tmem, tD2 = tmem + 128;  // D1: 2 x 64 columns, D2: 2 x npad columns
+    griddep_wait();
+    griddep_launch_dependents();
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int stage = 0, seg = 0;
+            uint32_t phase = 0;
+            for (long long b = lo; b < hi;) {
+                const int t = (int)(b / p.kblocks);
+                const long long e = min(hi, (long long)(t + 1) * p.kblocks);
+                // the factor tile of this row tile (MMA1's A), once per segment
+                if (!mbar_wait(a1empty, (uint32_t)((seg & 1) ^ 1), p.err, kErrWaitEmpty)) break;
+                mbar_arrive_expect_tx(a1full, (uint32_t)(p.nbox * 16384));
+                for (int q = 0; q < p.nbox; q++) tma_load_2d(sA1 + q * 16384, &tmA1, q * 64, t * kTileM, a1full);
+                bool ok = true;
+                for (long long bb = b; bb < e; bb++) {
+                    const int kb = (int)(bb % p.kblocks);
+                    if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&full[stage], (uint32_t)stageBytes);
+                    tma_load_2d(sV(stage), &tmV, kb * kBlockK, t * kTileM, &full[stage]);
+                    for (int q = 0; q < p.nbox; q++)
+                        tma_load_2d(sB1(stage) + q * 8192, &tmB1, q * 64, kb * kBlockK, &full[stage]);
+                    tma_load_2d(sB2(stage), &tmB2, kb * kBlockK, 0, &full[stage]);
+                    if (++stage == p.stages) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+                if (!ok) break;
+                seg++;
+                b = e;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t id1 = idesc_bf16_f32(kTileM, 64), id2 = idesc_bf16_f32(kTileM, p.npad);
+            int stage = 0, seg = 0;
+            uint32_t phase = 0;
+            long long g = 0;  // global block counter (D1 / R double buffers)
+            bool ok = true;
+            int prev_stage = 0;
+            for (long long b = lo; b < hi && ok;) {
+                const int t = (int)(b / p.kblocks);
+                const long long e = min(hi, (long long)(t + 1) * p.kblocks);
+                const int acc = seg & 1;
+                if (!mbar_wait(a1full, (uint32_t)(seg & 1), p.err, kErrWaitFull)) break;
+                if (!mbar_wait(&tempty[acc], (uint32_t)(((seg >> 1) & 1) ^ 1), p.err, kErrWaitTmemEmpty)) break;
+                tc_fence_after();
+                const uint32_t a1 = smem_u32(sA1);
+                bool first2 = true;
+                for (long long bb = b; bb <= e && ok; bb++) {
+                    if (bb < e) {
+                        // MMA1 for block g
+                        const int db = (int)(g & 1);
+                        if (!mbar_wait(&full[stage], phase, p.err, kErrWaitFull) ||
+                            !mbar_wait(&d1empty[db], (uint32_t)(((g >> 1) & 1) ^ 1), p.err, kErrWaitTmemEmpty)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t b1 = smem_u32(sB1(stage));
+                        for (int k16 = 0; k16 < p.npad / 16; k16++) {
+                            const int q = k16 >> 2, w = (k16 & 3) * 32;
+                            tc_mma_f16(tD1 + (uint32_t)(db * 64), smem_desc(a1 + q * 16384 + w, 16, 1024, 2),
+                                       smem_desc(b1 + q * 8192 + w, 16, 1024, 2), id1, k16 > 0 ? 1u : 0u);
+                        }
+                        tc_commit(&d1full[db]);
+                    }
+                    if (bb > b) {
+                        // MMA2 for block g-1 (its R is formed by the epilogue warps)
+                        const long long gp = g - 1;
+                        const int rb = (int)(gp & 1);
+                        if (!mbar_wait(&rfull[rb], (uint32_t)((gp >> 1) & 1), p.err, kErrWaitFull)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t ra = smem_u32(sR + rb * 16384), b2 = smem_u32(sB2(prev_stage));
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            tc_mma_f16(tD2 + (uint32_t)(acc * p.npad), smem_desc(ra + k * 32, 16, 1024, 2),
+                                       smem_desc(b2 + k * 32, 16, 1024, 2), id2, (first2 && k == 0) ? 0u : 1u);
+                        first2 = false;
+                        tc_commit(&empty[prev_stage]);
+                        tc_commit(&rempty[rb]);
+                    }
+                    if (bb < e) {
+                        prev_stage = stage;
+                        if (++stage == p.stages) {
+                            stage = 0;
+                            phase ^= 1;
+                        }
+                        g++;
+                    }
+                }
+                if (!ok) break;
+                tc_commit(&tfull[acc]);
+                tc_commit(a1empty);
+                seg++;
+                b = e;
+            }
+            tc_commit(mdone);
+            mbar_wait_quiet(mdone, 0);
+        }
+    } else {
+        // finish the denominators (column / row sums of the other factor) from the partials
+        if (p.sum_out) {
+            const int et = threadIdx.x - 64;
+            const int E = p.npad;
+            const int e0 = (int)((long long)blockIdx.x * E / gridDim.x), e1 = (int)((long long)(blockIdx.x + 1) * E / gridDim.x);
+            for (int eb = e0; eb < e1; eb += 32) {
+                const int ei = eb + (et >> 2);
+                float sacc = 0.f;
+                if (ei < e1) {
+                    int z = et & 3;
+                    for (; z + 28 < p.sum_count; z += 32) {
+                        float v[8];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) v[q] = p.sum_partials[(size_t)(z + 4 * q) * E + ei];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) sacc += v[q];
+                    }
+                    for (; z < p.sum_count; z += 4) sacc += p.sum_partials[(size_t)z * E + ei];
+                }
+                sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
+                sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
+                if (ei < e1 && (et & 3) == 0) p.sum_out[ei] = sacc;
+            }
+        }
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+        int stage = 0, seg = 0;
+        long long g = 0;
+        for (long long b = lo; b < hi;) {
+            const int t = (int)(b / p.kblocks);
+            const long long e = min(hi, (long long)(t + 1) * p.kblocks);
+            bool ok = true;
+            for (long long bb = b; bb < e; bb++) {
+                const int db = (int)(g & 1);
+                if (!warp_wait(&d1full[db], (uint32_t)((g >> 1) & 1), p.err, kErrWaitTmemFull) ||
+                    !warp_wait(&full[stage], (uint32_t)((g / p.stages) & 1), p.err, kErrWaitFull) ||
+                    !warp_wait(&rempty[db], (uint32_t)(((g >> 1) & 1) ^ 1), p.err, kErrWaitEmpty)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const unsigned char *vt = sV(stage);
+                unsigned char *rt = sR + db * 16384;
+#pragma unroll
+                for (int c16 = 0; c16 < 4; c16++) {  // 16 columns of S at a time
+                    float sv[16];
+                    tmem_ld16(tD1 + (uint32_t)(db * 64) + lane_off + (uint32_t)(c16 * 16), sv);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {  // two 16-byte chunks of 8 values
+                        const int chunk = c16 * 2 + h;
+                        const uint4 vraw = *reinterpret_cast<const uint4 *>(vt + sw128(row, chunk));
+                        const __nv_bfloat16 *vv = reinterpret_cast<const __nv_bfloat16 *>(&vraw);
+                        uint4 out;
+                        __nv_bfloat16 *ov = reinterpret_cast<__nv_bfloat16 *>(&out);
+#pragma unroll
+                        for (int q = 0; q < 8; q++) {
+                            const float v = __bfloat162float(vv[q]);
+                            const float rr = v == 0.f ? 0.f : v / (sv[h * 8 + q] + p.eps);
+                            ov[q] = __float2bfloat16_rn(rr);
+                        }
+                        *reinterpret_cast<uint4 *>(rt + sw128(row, chunk)) = out;
+                    }
+                }
+                // R written with ordinary stores: make it visible to the tensor core, then hand it over
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(&rfull[db]);
+                    mbar_arrive(&d1empty[db]);
+                }
+                if (++stage == p.stages) stage = 0;
+                g++;
+            }
+            if (!ok) break;
+            const int acc = seg & 1;
+            if (!warp_wait(&tfull[acc], (uint32_t)((seg >> 1) & 1), p.err, kErrWaitTmemFull)) break;
+            tc_fence_after();
+            float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
+            for (int c = 0; c < p.npad; c += 16) {
+                float v[16];
+                tmem_ld16(tD2 + (uint32_t)(acc * p.npad) + lane_off + (uint32_t)c, v);
+                tmem_ld_wait();
+                float4 *d4 = reinterpret_cast<float4 *>(dst + c);
+                d4[0] = make_float4(v[0], v[1], v[2], v[3]);
+                d4[1] = make_float4(v[4], v[5], v[6], v[7]);
+                d4[2] = make_float4(v[8], v[9], v[10], v[11]);
+                d4[3] = make_float4(v[12], v[13], v[14], v[15]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[acc]);
+            seg++;
+            b = e;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, p.tmem_cols);
+    }
+}
+
+// KL update (nmf_kernels.cu:289,337 with the eps clamp of :104,190): X *= num / max(sum, eps)
+// on a 16-wide tile; writes X, its two BF16 copies, and this tile's partial sums over its columns
+// (the other half-step's denominator).
+struct KlUpdParams {
+    float *X;
+    __nv_bfloat16 *Xb;   // element (a, c) at a*ldb + c   (Hb row-major / Wb column-major)
+    long long ldb;
+    __nv_bfloat16 *Xr;   // element (a, c) at c*ldr + a   (Hc column-major H / Wr row-major W)
+    long long ldr;
+    long long ldx;       // W: n
+    const float *sums;   // [npad] denominators (before the eps clamp)
+    const float *P;
+    const int *slot_ptr, *slot_list, *tile_slots;
+    float *sum_partials; // [cta][npad]
+    int r, cols, npad;
+    float eps;
+    int update;
+};
+
+template <int RP, bool IS_W>
+__global__ void __launch_bounds__(kUpdThreads) tc_kl_update_kernel(KlUpdParams p) {
+    constexpr int LDX = kUpdCols + 1;
+    __shared__ float Xs[RP * LDX];
+    __shared__ float sumS[RP];
+    const int tid = threadIdx.x;
+    const int c0 = blockIdx.x * kUpdCols;
+    const int ncol = min(kUpdCols, p.cols - c0);
+    const int r = p.r;
+    griddep_wait();
+    griddep_launch_dependents();
+    constexpr int XL = RP * kUpdCols / kUpdThreads;
+    float xv[XL], acc[XL];
+#pragma unroll
+    for (int j = 0; j < XL; j++) {
+        const int k = tid + j * kUpdThreads;
+        if (IS_W) {
+            const int a = k / kUpdCols, c = k % kUpdCols;
+            xv[j] = (a < r && c < ncol) ? p.X[(long long)a * p.ldx + c0 + c] : 0.f;
+        } else {
+            const int c = k / RP, a = k % RP;
+            xv[j] = (a < r && c < ncol) ? p.X[(long long)(c0 + c) * r + a] : 0.f;
+        }
+        acc[j] = 0.f;
+    }
+    if (tid < RP) sumS[tid] = p.update ? fmaxf(p.sums[tid], p.eps) : 1.f;
+    if (p.update) {
+        const int tile = c0 / 128, lrow0 = c0 % 128;
+        auto add_slot = [&](int sl) {
+            const float *bs = p.P + ((size_t)sl * 128 + lrow0) * p.npad;
+#pragma unroll
+            for (int j = 0; j < XL; j++) {
+                const int k = tid + j * kUpdThreads;
+                int a, c;
+                if (IS_W) { a = k / kUpdCols; c = k % kUpdCols; }
+                else      { c = k / RP; a = k % RP; }
+                if (c < ncol) acc[j] += bs[c * p.npad + a];
+            }
+        };
+        if (p.tile_slots) {
+            const int4 *ts = reinterpret_cast<const int4 *>(p.tile_slots + (size_t)tile * kSlotW);
+            const int4 sa = ts[0], sb = ts[1];
+            const int sl[kSlotW] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+#pragma unroll
+            for (int q = 0; q < kSlotW; q++)
+                if (sl[q] >= 0) add_slot(sl[q]);
+        } else {
+            for (int q = p.slot_ptr[tile]; q < p.slot_ptr[tile + 1]; q++) add_slot(p.slot_list[q]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < XL; j++) {
+        const int k = tid + j * kUpdThreads;
+        int a, c;
+        if (IS_W) { a = k / kUpdCols; c = k % kUpdCols; }
+        else      { c = k / RP; a = k % RP; }
+        float x = xv[j];
+        if (p.update && a < r && c < ncol) {
+            x *= (acc[j] / sumS[a]);
+            if (IS_W) p.X[(long long)a * p.ldx + c0 + c] = x;
+            else p.X[(long long)(c0 + c) * r + a] = x;
+        }
+        Xs[a * LDX + c] = x;
+    }
+    __syncthreads();
+    if (p.update) {
+        for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {  // Xb: c fastest
+            const int a = k / kUpdCols, c = k % kUpdCols;
+            if (a < r && c < ncol) p.Xb[(long long)a * p.ldb + c0 + c] = __float2bfloat16_rn(Xs[a * LDX + c]);
+        }
+        for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {  // Xr: a fastest
+            const int c = k / RP, a = k % RP;
+            if (c < ncol) p.Xr[(long long)(c0 + c) * p.ldr + a] = __float2bfloat16_rn(a < r ? Xs[a * LDX + c] : 0.f);
+        }
+    }
+    if (tid < RP) {
+        float sacc = 0.f;
+        for (int c = 0; c < kUpdCols; c++) sacc += Xs[tid * LDX + c];
+        p.sum_partials[(size_t)blockIdx.x * RP + tid] = sacc;
+    }
+}
+
+// W (n x r FP32) -> Wr (row-major BF16, ld ldr, zero beyond r); H (r x m) -> Hc (column-major BF16)
+__global__ void convert_rowmajor_kernel(const float *__restrict__ X, int rows, int r, long long ldx_rows,
+                                        bool x_is_w, __nv_bfloat16 *__restrict__ Xr, long long ldr) {
+    long long total = (long long)rows * ldr;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long c = k / ldr, a = k % ldr;
+        float v = 0.f;
+        if (a < r) v = x_is_w ? X[a * ldx_rows + c] : X[c * r + a];
+        Xr[k] = __float2bfloat16_rn(v);
+    }
+}
+
 }  // namespace gpunmf
 
 struct TcGemm {
@@ -538,8 +955,20 @@ struct TcGemm {
     int *tile_slots = nullptr;
 };
 
+struct KlGemm {
+    CUtensorMap tmV, tmA1, tmB1, tmB2;
+    gpunmf::KlParams p;
+    int grid = 0, smem = 0;
+    int *slot_ptr = nullptr, *slot_list = nullptr, *tile_slots = nullptr;
+};
+
 struct TcState {
     __nv_bfloat16 *Vb = nullptr, *Vbt = nullptr, *Wb = nullptr, *Hb = nullptr;
+    // KL rule: second BF16 layouts (W row-major, H column-major), denominators and their partials
+    __nv_bfloat16 *Wr = nullptr, *Hc = nullptr;
+    long long ldr = 0;
+    KlGemm kh, kw;
+    float *S_w = nullptr, *S_h = nullptr, *SP_w = nullptr, *SP_h = nullptr;
     long long ldv = 0, ldvt = 0, ldw = 0, ldh = 0;
     int npad = 16;
     TcGemm gh, gw;  // H-step (W'V) and W-step (VH')
@@ -773,25 +1202,204 @@ static UpdParams update_params_w(gpunmf_job *j, int update) {
     return u;
 }
 
-gpunmf_status tc_supported(int rule, int n, int m, int r) {
-    if (rule != GPUNMF_EUCLIDEAN) {
-        set_error("BF16 tensor-core path covers the Euclidean rule");
+constexpr int kKlSmemBudget = 220 * 1024;
+constexpr int kKlMaxRank = 128;
+
+static cudaError_t set_kl_smem_once() {
+    static std::once_flag once;
+    static cudaError_t result = cudaSuccess;
+    std::call_once(once, [] {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        result = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (result == cudaSuccess)
+            result = cudaFuncSetAttribute(tc_kl_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    });
+    return result;
+}
+
+static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npad, float **partials, int *err) {
+    const int tiles = ceil_div(rows, kTileM);
+    const int kblocks = ceil_div(K, kBlockK);
+    const long long T = (long long)tiles * kblocks;
+    g.grid = (int)std::min<long long>(num_sms(), T);
+    std::vector<int> ptr, list;
+    int max_seg = 1;
+    schedule(tiles, kblocks, g.grid, &max_seg, ptr, list);
+    bool table_ok = true;
+    for (int t = 0; t < tiles; t++)
+        if (ptr[t + 1] - ptr[t] > kSlotW) table_ok = false;
+    std::vector<int> table;
+    if (table_ok) {
+        table.assign((size_t)tiles * kSlotW, -1);
+        for (int t = 0; t < tiles; t++)
+            for (int q = ptr[t]; q < ptr[t + 1]; q++) table[(size_t)t * kSlotW + (q - ptr[t])] = list[q];
+    }
+    const int nbox = (npad + 63) / 64;
+    const int stage_bytes = 16384 + nbox * 8192 + npad * 128;
+    const int fixed = 1024 + nbox * 16384 + 2 * 16384 + 512;
+    const int stages = std::min(kMaxStages, (kKlSmemBudget - fixed) / stage_bytes);
+    if (stages < 2) {
+        set_error("KL tensor-core kernel: rank too large for the shared-memory pipeline");
         return GPUNMF_ERR_UNSUPPORTED;
+    }
+    g.p.tiles = tiles;
+    g.p.kblocks = kblocks;
+    g.p.npad = npad;
+    g.p.stages = stages;
+    g.p.max_seg = max_seg;
+    g.p.nbox = nbox;
+    g.p.tmem_cols = (128 + 2 * npad) <= 256 ? 256 : 512;
+    g.p.eps = j->eps;
+    g.p.err = err;
+    g.smem = fixed + stages * stage_bytes;
+    size_t slots = (size_t)g.grid * max_seg;
+    cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_ptr, ptr.size() * sizeof(int));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_list, std::max<size_t>(1, list.size()) * sizeof(int));
+    if (e == cudaSuccess) e = job_h2d(j, g.slot_ptr, ptr.data(), ptr.size() * sizeof(int));
+    if (e == cudaSuccess && !list.empty()) e = job_h2d(j, g.slot_list, list.data(), list.size() * sizeof(int));
+    if (e == cudaSuccess && table_ok) {
+        e = job_dev_alloc(j, (void **)&g.tile_slots, table.size() * sizeof(int));
+        if (e == cudaSuccess) e = job_h2d(j, g.tile_slots, table.data(), table.size() * sizeof(int));
+    }
+    if (e != cudaSuccess) {
+        set_error("KL tensor-core workspace allocation failed: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return GPUNMF_ERR_NOMEM;
+    }
+    g.p.partials = *partials;
+    return GPUNMF_OK;
+}
+
+static cudaError_t launch_kl_gemm(KlGemm &g, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.grid);
+    cfg.blockDim = dim3(kGemmThreads);
+    cfg.dynamicSmemBytes = g.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, tc_kl_gemm_kernel, g.tmV, g.tmA1, g.tmB1, g.tmB2, g.p);
+}
+
+static cudaError_t launch_kl_update(const KlUpdParams &u, int rp, bool is_w, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ceil_div(u.cols, kUpdCols));
+    cfg.blockDim = dim3(kUpdThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    switch (rp) {
+#define CASE(R)                                                                          \
+    case R:                                                                              \
+        return is_w ? cudaLaunchKernelEx(&cfg, tc_kl_update_kernel<R, true>, u)          \
+                    : cudaLaunchKernelEx(&cfg, tc_kl_update_kernel<R, false>, u);
+        CASE(16) CASE(32) CASE(48) CASE(64) CASE(80) CASE(96) CASE(112) CASE(128)
+#undef CASE
+    }
+    return cudaErrorInvalidValue;
+}
+
+static KlUpdParams kl_params_h(gpunmf_job *j, int update) {
+    TcState *t = j->tc;
+    KlUpdParams u{};
+    u.X = j->H; u.Xb = t->Hb; u.ldb = t->ldh; u.Xr = t->Hc; u.ldr = t->ldr; u.ldx = 0;
+    u.sums = t->S_w; u.P = t->P_h;
+    u.slot_ptr = t->kh.slot_ptr; u.slot_list = t->kh.slot_list; u.tile_slots = t->kh.tile_slots;
+    u.sum_partials = t->SP_h;
+    u.r = j->r; u.cols = j->m; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    return u;
+}
+
+static KlUpdParams kl_params_w(gpunmf_job *j, int update) {
+    TcState *t = j->tc;
+    KlUpdParams u{};
+    u.X = j->W; u.Xb = t->Wb; u.ldb = t->ldw; u.Xr = t->Wr; u.ldr = t->ldr; u.ldx = j->n;
+    u.sums = t->S_h; u.P = t->P_w;
+    u.slot_ptr = t->kw.slot_ptr; u.slot_list = t->kw.slot_list; u.tile_slots = t->kw.tile_slots;
+    u.sum_partials = t->SP_w;
+    u.r = j->r; u.cols = j->n; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    return u;
+}
+
+static gpunmf_status tc_create_kl(gpunmf_job *j) {
+    TcState *t = j->tc;
+    const int n = j->n, m = j->m, r = j->r;
+    t->ldr = t->npad;
+    const int cw = ceil_div(n, kUpdCols), ch = ceil_div(m, kUpdCols);
+    cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->ldv * m * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->ldvt * n * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hb, (size_t)t->ldh * r * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wr, (size_t)n * t->ldr * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hc, (size_t)m * t->ldr * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->err, sizeof(int));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->S_w, t->npad * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->S_h, t->npad * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->SP_w, (size_t)cw * t->npad * sizeof(float));
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->SP_h, (size_t)ch * t->npad * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemsetAsync(t->err, 0, sizeof(int), j->stream);
+    if (e != cudaSuccess) {
+        set_error("KL tensor-core buffers: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return GPUNMF_ERR_NOMEM;
+    }
+    gpunmf_status st = setup_kl(j, t->kh, m, n, t->npad, &t->P_h, t->err);
+    if (st == GPUNMF_OK) st = setup_kl(j, t->kw, n, m, t->npad, &t->P_w, t->err);
+    if (st != GPUNMF_OK) return st;
+    t->kh.p.sum_partials = t->SP_w; t->kh.p.sum_out = t->S_w; t->kh.p.sum_count = cw;
+    t->kw.p.sum_partials = t->SP_h; t->kw.p.sum_out = t->S_h; t->kw.p.sum_count = ch;
+    // H-step: rows u; V tile from Vb, A1 = Hc rows u, B1 = Wr rows i, B2 = Wb
+    st = make_map(&t->kh.tmV, t->Vb, n, m, t->ldv, kTileM);
+    if (st == GPUNMF_OK) st = make_map(&t->kh.tmA1, t->Hc, r, m, t->ldr, kTileM);
+    if (st == GPUNMF_OK) st = make_map(&t->kh.tmB1, t->Wr, r, n, t->ldr, kBlockK);
+    if (st == GPUNMF_OK) st = make_map(&t->kh.tmB2, t->Wb, n, r, t->ldw, t->npad);
+    // W-step: rows i; V tile from Vbt, A1 = Wr rows i, B1 = Hc rows u, B2 = Hb
+    if (st == GPUNMF_OK) st = make_map(&t->kw.tmV, t->Vbt, m, n, t->ldvt, kTileM);
+    if (st == GPUNMF_OK) st = make_map(&t->kw.tmA1, t->Wr, r, n, t->ldr, kTileM);
+    if (st == GPUNMF_OK) st = make_map(&t->kw.tmB1, t->Hc, r, m, t->ldr, kBlockK);
+    if (st == GPUNMF_OK) st = make_map(&t->kw.tmB2, t->Hb, m, r, t->ldh, t->npad);
+    if (st != GPUNMF_OK) return st;
+    GPUNMF_CUDA_TRY(set_kl_smem_once());
+    return GPUNMF_OK;
+}
+
+gpunmf_status tc_supported(int rule, int n, int m, int r) {
+    (void)n;
+    (void)m;
+    if (rule == GPUNMF_DIVERGENCE) {
+        if (r > kKlMaxRank) {
+            set_error("BF16 KL path supports r <= %d", kKlMaxRank);
+            return GPUNMF_ERR_UNSUPPORTED;
+        }
+        return GPUNMF_OK;
     }
     if (r > kMaxRank) {
         set_error("BF16 path supports r <= %d", kMaxRank);
         return GPUNMF_ERR_UNSUPPORTED;
     }
-    (void)n;
-    (void)m;
     return GPUNMF_OK;
 }
 
 void tc_add_sizes(int, int, int, int, size_t *) {}
 
 size_t tc_footprint(int rule, int n, int m, int r) {
-    (void)rule;
     const int npad = npad_of(r);
+    if (rule == GPUNMF_DIVERGENCE) {
+        size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r +
+                        (size_t)(n + m) * npad);
+        b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
+        b += (size_t)npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
+        return b;
+    }
     size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r);
     b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
     b += (size_t)npad * npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
@@ -808,6 +1416,7 @@ gpunmf_status tc_create(gpunmf_job *j) {
     t->ldvt = ceil8(m);
     t->ldw = ceil8(n);
     t->ldh = ceil8(m);
+    if (j->rule == GPUNMF_DIVERGENCE) return tc_create_kl(j);
     cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->ldv * m * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->ldvt * n * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
@@ -866,6 +1475,16 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
     convert_h_kernel<<<std::min(1024, ceil_div((long long)j->r * j->m, 256)), 256, 0, s>>>(j->H, j->r, j->m,
                                                                                           t->Hb, t->ldh);
     GPUNMF_CUDA_TRY(cudaGetLastError());
+    if (j->rule == GPUNMF_DIVERGENCE) {
+        convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->n * t->ldr, 256)), 256, 0, s>>>(
+            j->W, j->n, j->r, j->n, true, t->Wr, t->ldr);
+        convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->m * t->ldr, 256)), 256, 0, s>>>(
+            j->H, j->m, j->r, 0, false, t->Hc, t->ldr);
+        GPUNMF_CUDA_TRY(cudaGetLastError());
+        // column sums of the initial W, finished by the first H-step kernel
+        GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 0), t->npad, true, s));
+        return GPUNMF_OK;
+    }
     // Gram partials of the initial W, finished by the first H-step GEMM
     GPUNMF_CUDA_TRY(launch_update(update_params_w(j, 0), t->npad, true, s));
     return GPUNMF_OK;
@@ -891,6 +1510,22 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
     {
         gpunmf_status st = job_quality_step(j, true);
         if (st != GPUNMF_OK) return st;
+    }
+    if (j->rule == GPUNMF_DIVERGENCE) {
+        // H <- H .* [W'(V ./ (WH + eps))] ./ max(colsum W, eps); the kernel also finishes colsum W
+        mark_begin(j);
+        GPUNMF_CUDA_TRY(launch_kl_gemm(t->kh, s));
+        mark_end(j);
+        GPUNMF_CUDA_TRY(launch_kl_update(kl_params_h(j, 1), t->npad, false, s));
+        j->launches += 2;
+        if (!updateW) return GPUNMF_OK;
+        // W <- W .* [(V ./ (WH + eps)) H'] ./ max(rowsum H, eps) with the new H
+        mark_begin(j);
+        GPUNMF_CUDA_TRY(launch_kl_gemm(t->kw, s));
+        mark_end(j);
+        GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 1), t->npad, true, s));
+        j->launches += 2;
+        return GPUNMF_OK;
     }
     // H <- H .* (W'V) ./ (W'W H + eps); the GEMM also finishes W'W
     mark_begin(j);
@@ -924,7 +1559,9 @@ void tc_destroy(gpunmf_job *j) {
     if (!t) return;
     void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h, t->G_w, t->GP_h, t->GP_w,
                     t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list,
-                    t->gh.tile_slots, t->gw.tile_slots};
+                    t->gh.tile_slots, t->gw.tile_slots, t->Wr, t->Hc, t->S_w, t->S_h, t->SP_w, t->SP_h,
+                    t->kh.slot_ptr, t->kh.slot_list, t->kh.tile_slots, t->kw.slot_ptr, t->kw.slot_list,
+                    t->kw.tile_slots};
     for (void *p : ptrs) job_dev_free(j, p);
     delete t;
     j->tc = nullptr;

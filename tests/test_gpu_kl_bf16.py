@@ -1,0 +1,92 @@
+"""BF16 tensor-core path of the KL rule (fused S = WH -> R = V/(S+eps) -> numerator).
+
+1. One iteration against an exact emulation: S from BF16-rounded W and H, R = V_bf16/(S+eps) rounded to
+   BF16, numerators from R and the BF16 factor, denominators max(sum, eps) in FP32 -> the GPU result may
+   differ only by accumulation order (bound 2e-5 relative Frobenius).
+2. Over many iterations it tracks the FP32 KL path (residuals within 1e-3) and the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel
+from gpumlib_gb300 import inputs
+from test_gpu_bf16 import bf16
+
+pytestmark = pytest.mark.gpu
+
+
+def emulate_kl_one(V, W, H, eps, H1_gpu):
+    Vb, Wb, Hb = bf16(V), bf16(W), bf16(H)
+    Wd, Hd = W.astype(np.float64), H.astype(np.float64)
+    S = Wb @ Hb
+    R = bf16((Vb / (S + eps)).astype(np.float32))
+    sw = np.maximum(Wd.sum(axis=0), eps)
+    H1 = Hd * (Wb.T @ R) / sw[:, None]
+    H1b = bf16(H1_gpu)
+    S2 = Wb @ H1b
+    R2 = bf16((Vb / (S2 + eps)).astype(np.float32))
+    sh = np.maximum(H1_gpu.astype(np.float64).sum(axis=1), eps)
+    W1 = Wd * (R2 @ H1b.T) / sh[None, :]
+    return W1, H1
+
+
+SHAPES = [(512, 384, 16), (1000, 777, 20), (300, 1300, 7), (129, 65, 1), (2048, 1024, 128), (513, 700, 100),
+          (64, 4096, 64), (37, 11, 3)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["%dx%dr%d" % s for s in SHAPES])
+def test_kl_one_iteration_matches_emulation(gpu, shape):
+    n, m, r = shape
+    g = np.random.Generator(np.random.PCG64(n + m + r))
+    V = np.asfortranarray(g.poisson(2.0, size=(n, m)).astype(np.float32))
+    W, H = inputs.factors(90 + n, n, m, r)
+    eps = np.float32(1e-9)
+    with gpu.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision="bf16", quality_interval=0) as nmf:
+        nmf.DoIteration()
+        W1g, H1g = nmf.GetW(), nmf.GetH()
+    W1, H1 = emulate_kl_one(V, W, H, float(eps), H1g)
+    assert rel(H1g, H1) <= 2e-5, "H-step (fused KL tcgen05) differs"
+    assert rel(W1g, W1) <= 2e-5, "W-step (fused KL tcgen05) differs"
+
+
+def test_kl_bf16_tracks_fp32(gpu):
+    n, m, r = 2048, 1536, 64
+    g = np.random.Generator(np.random.PCG64(7))
+    P = g.gamma(0.3, 1.0, size=(n, 64))
+    Q = g.gamma(0.3, 1.0, size=(64, m))
+    V = np.asfortranarray(g.poisson(P @ Q).astype(np.float32))
+    W, H = inputs.factors(8, n, m, r)
+    res = {}
+    for prec in ("fp32", "bf16"):
+        with gpu.NMF_MultiplicativeDivergence(V, W, H, eps=1e-9, precision=prec, quality_interval=0) as nmf:
+            nmf.Iterate(100)
+            res[prec] = (nmf.Residual(), nmf.ObjectiveKL())
+    assert abs(res["bf16"][0] - res["fp32"][0]) <= 1e-3, res
+    assert abs(res["bf16"][1] - res["fp32"][1]) <= 1e-3 * abs(res["fp32"][1]), res
+
+
+def test_kl_bf16_error_vs_f64_oracle(gpu):
+    n, m, r = 700, 500, 12
+    g = np.random.Generator(np.random.PCG64(9))
+    V = np.asfortranarray(g.poisson(3.0, size=(n, m)).astype(np.float32))
+    W, H = inputs.factors(10, n, m, r)
+    with gpu.NMF_MultiplicativeDivergence(V, W, H, eps=1e-9, precision="bf16", quality_interval=0) as nmf:
+        nmf.Iterate(20)
+        Wg, Hg = nmf.GetW(), nmf.GetH()
+    Wd, Hd = oracle.f64_run(1, V, W, H, 20, eps=1e-9, nthreads=8)
+    assert rel(Wg.astype(np.float64) @ Hg, Wd @ Hd) <= 5e-3
+
+
+def test_kl_bf16_update_w_false_and_deterministic(gpu):
+    n, m, r = 900, 600, 32
+    g = np.random.Generator(np.random.PCG64(11))
+    V = np.asfortranarray(g.poisson(1.5, size=(n, m)).astype(np.float32))
+    W, H = inputs.factors(12, n, m, r)
+    outs = []
+    for _ in range(2):
+        with gpu.NMF_MultiplicativeDivergence(V, W, H, precision="bf16", quality_interval=0) as nmf:
+            nmf.Iterate(3)
+            nmf.DoIteration(updateW=False)
+            outs.append((nmf.GetW(), nmf.GetH()))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
