@@ -65,7 +65,8 @@ def parse():
                    help="iterations of the residual comparison job (0 = skip)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", choices=["large_euclidean", "batched", "serving"], default="large_euclidean")
+    p.add_argument("--workload", choices=["large_euclidean", "batched", "serving", "kl_counts"],
+                   default="large_euclidean")
     p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--serve-duration", type=float, default=5.0,
                    help="seconds of arrivals replayed (the full stream is 60)")
@@ -430,6 +431,70 @@ def run_batched(args, rank, world, local, dist):
 
 
 # ---------------------------------------------------------------------------
+# KL workload: V 16384 x 4096 Poisson counts, r = 128
+# ---------------------------------------------------------------------------
+KL_METRIC = "NMF iters/s, KL multiplicative update, V 16384x4096 Poisson counts, r=128"
+
+
+def run_kl(args, rank, world, local, dist):
+    import gpumlib_gb300 as g
+    from gpumlib_gb300 import inputs
+
+    cfg = inputs.kl_counts()
+    V, W, H, eps = cfg["V"], cfg["W"], cfg["H"], cfg["eps"]
+    n, m = V.shape
+    r = cfg["r"]
+    prec = args.precision or "bf16"
+    nmf = g.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision=prec, quality_interval=0)
+    nmf.Iterate(args.warmup)
+    nmf.Synchronize()
+    dist.barrier()
+    with ClockSampler(local) as clk:
+        t = nmf.TimeIterations(args.steps)
+    ms = dist.max(t["total_ms"])
+    value = world * args.steps / (ms / 1e3)
+    tk = nmf.TimeIterations(args.steps, kernel_timing=True)
+    nmf.close()
+    hbm, bf16_tf, src = peaks()
+    vbytes = 2 if prec == "bf16" else 4
+    per_launch = n * m * vbytes + (n + m) * r * vbytes * 2
+    flops = 4.0 * n * m * r  # S = W H block products and the numerator product
+    avg_ms = tk["kernel_ms"] / max(1, tk["kernel_launches"])
+    gbs = per_launch / (avg_ms / 1e3) / 1e9
+    tfs = flops / (avg_ms / 1e3) / 1e12
+    if prec == "bf16" and tfs / bf16_tf > gbs / hbm:
+        roof = {"bound": "tensor", "achieved": round(tfs, 1), "peak": bf16_tf, "unit": "TFLOP/s",
+                "frac": round(tfs / bf16_tf, 4)}
+    else:
+        roof = {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s", "frac": round(gbs / hbm, 4)}
+    roof.update({"traffic": None, "peak_source": src, "avg_launch_ms": round(avg_ms, 5),
+                 "kernel": "fused KL product (S = WH -> V/(S+eps) -> numerator)" if prec == "bf16" else
+                           "KL ratio SGEMM", "hbm_frac": round(gbs / hbm, 4),
+                 "tensor_frac": round(tfs / bf16_tf, 4) if prec == "bf16" else None})
+    out = {"metric": KL_METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if prec == "bf16" else "f32",
+           "data": "synthetic: V ~ Poisson(P Q), P 16384x128, Q 128x4096 ~ Gamma(0.3,1) (seed 4); W,H U[0,1)+1e-4 (seed 5)",
+           "config": {"workload": "kl_counts_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r, "rule": "kl",
+                      "precision": prec, "eps": eps, "zero_fraction": float(np.mean(V == 0)),
+                      "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16)" % (n * m * 4 >> 20, n * m * 2 >> 20)},
+           "clocks": clk.summary(), "gpu_launches": t["launches"], "roofline": roof}
+    if args.full_job_iters and rank == 0:
+        iters = min(args.full_job_iters, cfg["iters"])
+        res = {}
+        for pr in (["bf16", "fp32"] if prec == "bf16" else ["fp32"]):
+            with g.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision=pr, quality_interval=0) as j:
+                tt = j.TimeIterations(iters)
+                res[pr] = {"residual": j.Residual(), "kl_objective": j.ObjectiveKL(),
+                           "iters_per_s": round(iters / (tt["total_ms"] / 1e3), 2)}
+        out["full_job"] = {"iters": iters, **res}
+        if "bf16" in res:
+            out["full_job"]["residual_gap"] = abs(res["bf16"]["residual"] - res["fp32"]["residual"])
+            out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 2)
+    return out
+
+
+# ---------------------------------------------------------------------------
 # serving workload: Poisson arrivals, continuous batching
 # ---------------------------------------------------------------------------
 SERVE_METRIC = "NMF serving jobs/s and p50/p99 latency (Poisson arrivals, n,m log-uniform [64,4096], r U{8..64})"
@@ -502,6 +567,8 @@ def main():
             out = run_batched(args, rank, world, local, dist)
         elif args.workload == "serving":
             out = run_serving(args, rank, world, local, dist)
+        elif args.workload == "kl_counts":
+            out = run_kl(args, rank, world, local, dist)
         else:
             out = run_ours(args, rank, world, local, dist)
     finally:

@@ -558,7 +558,10 @@ __device__ __forceinline__ uint32_t sw128(int row, int chunk) {
     return (uint32_t)(row * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
-__global__ void __launch_bounds__(kGemmThreads, 1)
+constexpr int kKlEpiWarps = 16;  // two groups of 8 (even / odd K blocks); 2 per TMEM lane quarter in a group
+constexpr int kKlThreads = 64 + 32 * kKlEpiWarps;  // warp 0 TMA, warp 1 MMA, then the ratio epilogue
+
+__global__ void __launch_bounds__(kKlThreads, 1)
     tc_kl_gemm_kernel(const __grid_constant__ CUtensorMap tmV, const __grid_constant__ CUtensorMap tmA1,
                       const __grid_constant__ CUtensorMap tmB1, const __grid_constant__ CUtensorMap tmB2,
                       KlParams p) {
@@ -594,11 +597,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         mbar_init(a1empty, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&d1full[b], 1);
-            mbar_init(&d1empty[b], 4);
-            mbar_init(&rfull[b], 4);
+            mbar_init(&d1empty[b], kKlEpiWarps / 2);  // buffer b is handled by group b
+            mbar_init(&rfull[b], kKlEpiWarps / 2);
             mbar_init(&rempty[b], 1);
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], 4);
+            mbar_init(&tempty[b], kKlEpiWarps);
         }
         mbar_init(mdone, 1);
         fence_mbar_init();
@@ -726,10 +729,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     } else {
         // finish the denominators (column / row sums of the other factor) from the partials
         if (p.sum_out) {
-            const int et = threadIdx.x - 64;
+            const int et = threadIdx.x - 64;  // 0 .. 255
             const int E = p.npad;
             const int e0 = (int)((long long)blockIdx.x * E / gridDim.x), e1 = (int)((long long)(blockIdx.x + 1) * E / gridDim.x);
-            for (int eb = e0; eb < e1; eb += 32) {
+            for (int eb = e0; eb < e1; eb += kKlEpiWarps * 8) {
                 const int ei = eb + (et >> 2);
                 float sacc = 0.f;
                 if (ei < e1) {
@@ -748,10 +751,15 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 if (ei < e1 && (et & 3) == 0) p.sum_out[ei] = sacc;
             }
         }
-        const int quarter = warp & 3;
+        const int quarter = warp & 3;           // TMEM lanes this warp may access
+        const int grp = (warp - 2) >> 3;         // group 0 takes even K blocks, group 1 odd ones
+        const int part = ((warp - 2) >> 2) & 1;  // which 32 of the block's 64 columns
+        const int dpart = (warp - 2) >> 2;       // 0..3: share of the D2 drain
+        const float eps_pos = fmaxf(p.eps, 1e-30f);
         const int row = quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         int stage = 0, seg = 0;
+        uint32_t sphase = 0;
         long long g = 0;
         for (long long b = lo; b < hi;) {
             const int t = (int)(b / p.kblocks);
@@ -759,8 +767,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             bool ok = true;
             for (long long bb = b; bb < e; bb++) {
                 const int db = (int)(g & 1);
+                if (db != grp) {  // the other group's block: keep the counters in step
+                    if (++stage == p.stages) {
+                        stage = 0;
+                        sphase ^= 1;
+                    }
+                    g++;
+                    continue;
+                }
                 if (!warp_wait(&d1full[db], (uint32_t)((g >> 1) & 1), p.err, kErrWaitTmemFull) ||
-                    !warp_wait(&full[stage], (uint32_t)((g / p.stages) & 1), p.err, kErrWaitFull) ||
+                    !warp_wait(&full[stage], sphase, p.err, kErrWaitFull) ||
                     !warp_wait(&rempty[db], (uint32_t)(((g >> 1) & 1) ^ 1), p.err, kErrWaitEmpty)) {
                     ok = false;
                     break;
@@ -768,26 +784,34 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 tc_fence_after();
                 const unsigned char *vt = sV(stage);
                 unsigned char *rt = sR + db * 16384;
-#pragma unroll
-                for (int c16 = 0; c16 < 4; c16++) {  // 16 columns of S at a time
-                    float sv[16];
-                    tmem_ld16(tD1 + (uint32_t)(db * 64) + lane_off + (uint32_t)(c16 * 16), sv);
+                // this warp's 32 columns of S for its row: two loads in flight, one wait
+                float sv[32];
+                {
+                    float (&s0)[16] = *reinterpret_cast<float (*)[16]>(&sv[0]);
+                    float (&s1)[16] = *reinterpret_cast<float (*)[16]>(&sv[16]);
+                    const uint32_t ta = tD1 + (uint32_t)(db * 64 + part * 32) + lane_off;
+                    tmem_ld16(ta, s0);
+                    tmem_ld16(ta + 16, s1);
                     tmem_ld_wait();
+                }
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {  // two 16-byte chunks of 8 values
-                        const int chunk = c16 * 2 + h;
-                        const uint4 vraw = *reinterpret_cast<const uint4 *>(vt + sw128(row, chunk));
-                        const __nv_bfloat16 *vv = reinterpret_cast<const __nv_bfloat16 *>(&vraw);
-                        uint4 out;
-                        __nv_bfloat16 *ov = reinterpret_cast<__nv_bfloat16 *>(&out);
+                for (int cc = 0; cc < 4; cc++) {  // 16-byte chunks of 8 values
+                    const int chunk = part * 4 + cc;
+                    const uint4 vraw = *reinterpret_cast<const uint4 *>(vt + sw128(row, chunk));
+                    const __nv_bfloat162 *v2 = reinterpret_cast<const __nv_bfloat162 *>(&vraw);
+                    uint4 out;
+                    __nv_bfloat162 *o2 = reinterpret_cast<__nv_bfloat162 *>(&out);
 #pragma unroll
-                        for (int q = 0; q < 8; q++) {
-                            const float v = __bfloat162float(vv[q]);
-                            const float rr = v == 0.f ? 0.f : v / (sv[h * 8 + q] + p.eps);
-                            ov[q] = __float2bfloat16_rn(rr);
-                        }
-                        *reinterpret_cast<uint4 *>(rt + sw128(row, chunk)) = out;
+                    for (int q = 0; q < 4; q++) {
+                        // R is rounded to BF16 (8-bit significand): the approximate division
+                        // (2 ulp in FP32) is exact enough.  eps_pos > 0 keeps zero-padded
+                        // entries (V = 0, S = 0) at 0.
+                        const float2 vf = __bfloat1622float2(v2[q]);
+                        const float r0 = __fdividef(vf.x, sv[cc * 8 + 2 * q] + eps_pos);
+                        const float r1 = __fdividef(vf.y, sv[cc * 8 + 2 * q + 1] + eps_pos);
+                        o2[q] = __floats2bfloat162_rn(r0, r1);
                     }
+                    *reinterpret_cast<uint4 *>(rt + sw128(row, chunk)) = out;
                 }
                 // R written with ordinary stores: make it visible to the tensor core, then hand it over
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -797,7 +821,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                     mbar_arrive(&rfull[db]);
                     mbar_arrive(&d1empty[db]);
                 }
-                if (++stage == p.stages) stage = 0;
+                if (++stage == p.stages) {
+                    stage = 0;
+                    sphase ^= 1;
+                }
                 g++;
             }
             if (!ok) break;
@@ -805,7 +832,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             if (!warp_wait(&tfull[acc], (uint32_t)((seg >> 1) & 1), p.err, kErrWaitTmemFull)) break;
             tc_fence_after();
             float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
-            for (int c = 0; c < p.npad; c += 16) {
+            for (int c = dpart * 16; c < p.npad; c += 64) {  // the four warps of a quarter take turns by 16 columns
                 float v[16];
                 tmem_ld16(tD2 + (uint32_t)(acc * p.npad) + lane_off + (uint32_t)c, v);
                 tmem_ld_wait();
@@ -1275,7 +1302,7 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
 static cudaError_t launch_kl_gemm(KlGemm &g, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.grid);
-    cfg.blockDim = dim3(kGemmThreads);
+    cfg.blockDim = dim3(kKlThreads);
     cfg.dynamicSmemBytes = g.smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
