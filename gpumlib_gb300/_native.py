@@ -82,6 +82,12 @@ SIGNATURES = [
      [Dim3, Dim3] + [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3),
     ("gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_h", ctypes.c_int,
      [Dim3, Dim3] + [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3),
+    ("gpumlib_cuda_nmf_additive_euclidean_update_matrix", ctypes.c_int,
+     [ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("gpumlib_cuda_nmf_additive_divergence_update_matrix_w", ctypes.c_int,
+     [Dim3, Dim3] + [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3),
+    ("gpumlib_cuda_nmf_additive_divergence_update_matrix_h", ctypes.c_int,
+     [Dim3, Dim3] + [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3),
     ("gpumlib_nmf_sum_w", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     ("gpumlib_nmf_sum_h", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     ("gpumlib_nmf_quality", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,

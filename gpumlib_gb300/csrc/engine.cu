@@ -8,6 +8,13 @@
 //   KL (src/algorithms/nmf/nmf_multiplicative_divergence.cpp:29-50)
 //     WH = W H; quality(WH); H <- H .* [W' (V./(WH+eps))] ./ max(colsum W, eps);
 //     [WH = W H; W <- W .* [(V./(WH+eps)) H'] ./ max(rowsum H, eps)]
+//   additive Euclidean (src/algorithms/nmf/nmf_additive_euclidian.cpp:29-57)
+//     quality(W,H); H <- max(0, H + (H ./ W'W H) .* (W'V - W'W H));
+//     [W <- max(0, W + (W ./ W H H') .* (V H' - W H H'))]
+//     (the FIXED_H variant skips the H step, as the reference's GPU class does)
+//   additive KL (src/algorithms/nmf/nmf_additive_divergence.cpp:29-51)
+//     WH = W H; quality(WH); H <- max(0, H + (H ./ max(colsum W, eps)) .* W' (V./(WH+eps) - 1));
+//     [WH = W H; W <- max(0, W + (W ./ max(rowsum H, eps)) .* (V./(WH+eps) - 1) H')]
 // with the product arithmetic chosen per job: FP32 CUDA cores (the drop-in
 // path) or BF16 tensor cores (tc_kernels.cu).
 #include <stdarg.h>
@@ -106,10 +113,11 @@ static Sizes compute_sizes(int rule, int n, int m, int r, int precision) {
     z.s_g = sg1 > sg2 ? sg1 : sg2;
     z.p_h = (size_t)z.s_h * r * m;
     z.p_w = (size_t)z.s_w * n * r;
-    z.p_g = rule == GPUNMF_EUCLIDEAN ? (size_t)z.s_g * r * r : 0;
-    z.d_h = rule == GPUNMF_EUCLIDEAN ? (size_t)r * m : 0;
-    z.d_w = rule == GPUNMF_EUCLIDEAN ? (size_t)n * r : 0;
-    z.wh = rule == GPUNMF_DIVERGENCE ? (size_t)n * m : 0;
+    const bool kl = rule_is_kl(rule);
+    z.p_g = !kl ? (size_t)z.s_g * r * r : 0;
+    z.d_h = !kl ? (size_t)r * m : 0;
+    z.d_w = !kl ? (size_t)n * r : 0;
+    z.wh = kl ? (size_t)n * m : 0;
     size_t red = 2 * (size_t)wh_reduce_ctas(n, m);
     size_t red2 = (size_t)quality_ew_ctas((long long)n * m);
     z.red = red > red2 ? red : red2;
@@ -146,7 +154,7 @@ static void job_free(gpunmf_job *j) {
 static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int precision, void *stream,
                                gpunmf_job **out, unsigned char *pinned64 = nullptr, bool async_alloc = false) {
     *out = nullptr;
-    if (rule != GPUNMF_EUCLIDEAN && rule != GPUNMF_DIVERGENCE) {
+    if (!rule_valid(rule)) {
         set_error("unknown rule %d", rule);
         return GPUNMF_ERR_INVALID;
     }
@@ -315,50 +323,62 @@ void mark_end(gpunmf_job *j) {
 static gpunmf_status iterate_euclid_f32(gpunmf_job *j, bool updateW) {
     const int n = j->n, m = j->m, r = j->r;
     cudaStream_t s = j->stream;
+    const bool additive = j->rule != GPUNMF_EUCLIDEAN;
     TRY_STATUS(quality_step(j, true));
-    // H <- H .* (W'V) ./ (W'W H + eps)
-    mark_begin(j);
-    GPUNMF_CUDA_TRY(gemm_f32(r, m, n, {j->W, n, true}, {j->V, n, false}, j->P_h, r, j->s_h, s));
-    mark_end(j);
-    int sg = gemm_f32_splits(r, r, n);
-    GPUNMF_CUDA_TRY(gemm_f32(r, r, n, {j->W, n, true}, {j->W, n, false}, sg > 1 ? j->P_g : j->G, r, sg, s));
-    if (sg > 1) GPUNMF_CUDA_TRY(sum_partials(j->G, j->P_g, sg, (long long)r * r, s));
-    GPUNMF_CUDA_TRY(gemm_f32(r, m, r, {j->G, r, false}, {j->H, r, false}, j->D_h, r, 1, s));
-    GPUNMF_CUDA_TRY(euclid_update(j->H, j->P_h, j->s_h, j->D_h, (long long)r * m, j->eps, s));
-    j->launches += 4 + (sg > 1);
+    if (j->rule != GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H) {
+        // H <- H .* (W'V) ./ (W'W H + eps)   or the additive step on the same products
+        mark_begin(j);
+        GPUNMF_CUDA_TRY(gemm_f32(r, m, n, {j->W, n, true}, {j->V, n, false}, j->P_h, r, j->s_h, s));
+        mark_end(j);
+        int sg = gemm_f32_splits(r, r, n);
+        GPUNMF_CUDA_TRY(gemm_f32(r, r, n, {j->W, n, true}, {j->W, n, false}, sg > 1 ? j->P_g : j->G, r, sg, s));
+        if (sg > 1) GPUNMF_CUDA_TRY(sum_partials(j->G, j->P_g, sg, (long long)r * r, s));
+        GPUNMF_CUDA_TRY(gemm_f32(r, m, r, {j->G, r, false}, {j->H, r, false}, j->D_h, r, 1, s));
+        if (additive)
+            GPUNMF_CUDA_TRY(additive_update(j->H, j->P_h, j->s_h, j->D_h, (long long)r * m, s));
+        else
+            GPUNMF_CUDA_TRY(euclid_update(j->H, j->P_h, j->s_h, j->D_h, (long long)r * m, j->eps, s));
+        j->launches += 4 + (sg > 1);
+    }
     if (!updateW) return GPUNMF_OK;
-    // W <- W .* (V H') ./ (W H H' + eps)
+    // W <- W .* (V H') ./ (W H H' + eps)   or the additive step on the same products
     mark_begin(j);
     GPUNMF_CUDA_TRY(gemm_f32(n, r, m, {j->V, n, false}, {j->H, r, true}, j->P_w, n, j->s_w, s));
     mark_end(j);
-    sg = gemm_f32_splits(r, r, m);
-    GPUNMF_CUDA_TRY(gemm_f32(r, r, m, {j->H, r, false}, {j->H, r, true}, sg > 1 ? j->P_g : j->G, r, sg, s));
-    if (sg > 1) GPUNMF_CUDA_TRY(sum_partials(j->G, j->P_g, sg, (long long)r * r, s));
+    const int sgw = gemm_f32_splits(r, r, m);
+    GPUNMF_CUDA_TRY(gemm_f32(r, r, m, {j->H, r, false}, {j->H, r, true}, sgw > 1 ? j->P_g : j->G, r, sgw, s));
+    if (sgw > 1) GPUNMF_CUDA_TRY(sum_partials(j->G, j->P_g, sgw, (long long)r * r, s));
     GPUNMF_CUDA_TRY(gemm_f32(n, r, r, {j->W, n, false}, {j->G, r, false}, j->D_w, n, 1, s));
-    GPUNMF_CUDA_TRY(euclid_update(j->W, j->P_w, j->s_w, j->D_w, (long long)n * r, j->eps, s));
-    j->launches += 4 + (sg > 1);
+    if (additive)
+        GPUNMF_CUDA_TRY(additive_update(j->W, j->P_w, j->s_w, j->D_w, (long long)n * r, s));
+    else
+        GPUNMF_CUDA_TRY(euclid_update(j->W, j->P_w, j->s_w, j->D_w, (long long)n * r, j->eps, s));
+    j->launches += 4 + (sgw > 1);
     return GPUNMF_OK;
 }
 
 static gpunmf_status iterate_kl_f32(gpunmf_job *j, bool updateW) {
     const int n = j->n, m = j->m, r = j->r;
     cudaStream_t s = j->stream;
+    const bool additive = j->rule == GPUNMF_ADDITIVE_DIVERGENCE;
     GPUNMF_CUDA_TRY(gemm_f32(n, m, r, {j->W, n, false}, {j->H, r, false}, j->WH, n, 1, s));
     j->launches++;
     TRY_STATUS(quality_step(j, false));
     GPUNMF_CUDA_TRY(col_sums(j->W, n, r, j->eps, j->sums, s));
     mark_begin(j);
-    GPUNMF_CUDA_TRY(gemm_f32_ratio_right(r, m, n, {j->W, n, true}, j->V, j->WH, n, j->eps, j->P_h, j->s_h, s));
+    GPUNMF_CUDA_TRY(
+        gemm_f32_ratio_right(r, m, n, {j->W, n, true}, j->V, j->WH, n, j->eps, j->P_h, j->s_h, s, additive));
     mark_end(j);
-    GPUNMF_CUDA_TRY(kl_update(j->H, j->P_h, j->s_h, j->sums, (long long)r * m, 1, r, s));
+    GPUNMF_CUDA_TRY(kl_update(j->H, j->P_h, j->s_h, j->sums, (long long)r * m, 1, r, s, additive));
     j->launches += 3;
     if (!updateW) return GPUNMF_OK;
     GPUNMF_CUDA_TRY(gemm_f32(n, m, r, {j->W, n, false}, {j->H, r, false}, j->WH, n, 1, s));
     GPUNMF_CUDA_TRY(row_sums(j->H, r, m, j->eps, j->sums, s));
     mark_begin(j);
-    GPUNMF_CUDA_TRY(gemm_f32_ratio_left(n, r, m, j->V, j->WH, n, j->eps, {j->H, r, true}, j->P_w, j->s_w, s));
+    GPUNMF_CUDA_TRY(
+        gemm_f32_ratio_left(n, r, m, j->V, j->WH, n, j->eps, {j->H, r, true}, j->P_w, j->s_w, s, additive));
     mark_end(j);
-    GPUNMF_CUDA_TRY(kl_update(j->W, j->P_w, j->s_w, j->sums, (long long)n * r, n, r, s));
+    GPUNMF_CUDA_TRY(kl_update(j->W, j->P_w, j->s_w, j->sums, (long long)n * r, n, r, s, additive));
     j->launches += 4;
     return GPUNMF_OK;
 }
@@ -368,10 +388,10 @@ static gpunmf_status job_iterate(gpunmf_job *j, int iters, bool updateW) {
         gpunmf_status st;
         if (j->precision == GPUNMF_BF16)
             st = tc_iterate(j, updateW);
-        else if (j->rule == GPUNMF_EUCLIDEAN)
-            st = iterate_euclid_f32(j, updateW);
-        else
+        else if (rule_is_kl(j->rule))
             st = iterate_kl_f32(j, updateW);
+        else
+            st = iterate_euclid_f32(j, updateW);
         if (st != GPUNMF_OK) return st;
         j->iter_count++;
     }

@@ -56,6 +56,11 @@ struct gpunmf_job {
 };
 
 namespace gpunmf {
+// rule families: the Euclidean rules share products (W'V, W'W H, V H', W H H'), the KL rules a
+// stored WH and the ratio V/(WH+eps)
+inline bool rule_valid(int rule) { return rule >= GPUNMF_EUCLIDEAN && rule <= GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H; }
+inline bool rule_is_kl(int rule) { return rule == GPUNMF_DIVERGENCE || rule == GPUNMF_ADDITIVE_DIVERGENCE; }
+inline bool rule_is_additive(int rule) { return rule >= GPUNMF_ADDITIVE_EUCLIDEAN; }
 // device memory of a job: cudaMalloc / cudaFree, or cudaMallocAsync / cudaFreeAsync on the job's stream
 cudaError_t job_dev_alloc(gpunmf_job *j, void **p, size_t bytes);
 void job_dev_free(gpunmf_job *j, void *p);

@@ -3,10 +3,11 @@
 // The reference runs its factor products through cuBLAS SGEMM
 // (src/memory/DeviceMatrix.h:195-227) and its updates through the kernels of
 // src/cuda/nmf/nmf_kernels.cu.  Here one register-tiled SGEMM template covers
-// every product shape of both rules: operands are read through small "loader"
-// functors (plain column-major, transposed view, or the KL ratio V/(WH+eps)
-// formed on the fly), and the epilogue either stores, stores split-K partial
-// products, applies the KL update in place, or reduces a function of (V, WH)
+// every product shape of all four rules: operands are read through small
+// "loader" functors (plain column-major, transposed view, or the KL ratio
+// V/(WH+eps), or V/(WH+eps) - 1 for the additive KL rule, formed on the fly),
+// and the epilogue either stores, stores split-K partial products, applies a
+// KL update in place, or reduces a function of (V, WH)
 // into per-CTA FP64 partials (quality / residual) without storing WH.
 #include <math.h>
 
@@ -46,6 +47,17 @@ struct LdRatio {  // V(row,col) / (WH(row,col) + eps), both column-major with ld
     }
 };
 
+struct LdRatioM1 {  // V/(WH+eps) - 1: the additive KL gradient term (nmf_kernels_additive_divergence.cu:90,159)
+    const float *V, *WH;
+    long long ld;
+    float eps;
+    static constexpr bool kRowContig = true;
+    __device__ __forceinline__ float operator()(int row, int col) const {
+        long long o = (long long)col * ld + row;
+        return __ldg(V + o) / (__ldg(WH + o) + eps) - 1.0f;
+    }
+};
+
 // ------------------------------------------------------------------------
 // epilogues
 // ------------------------------------------------------------------------
@@ -66,6 +78,18 @@ struct EpiKLUpdate {  // X(i,j) *= c / sums[by_row ? i : j]   (nmf_kernels.cu:28
     __device__ __forceinline__ void operator()(int i, int j, float c, int) const {
         float *x = X + (long long)j * ldx + i;
         *x *= (c / sums[by_row ? i : j]);
+    }
+};
+struct EpiAKLUpdate {  // X(i,j) = max(0, x + (x / sums[..]) * c)  (nmf_kernels_additive_divergence.cu:101-104)
+    float *X;
+    long long ldx;
+    const float *sums;
+    bool by_row;
+    static constexpr bool kReduce = false;
+    __device__ __forceinline__ void operator()(int i, int j, float c, int) const {
+        float *x = X + (long long)j * ldx + i;
+        float v = *x + (*x / sums[by_row ? i : j]) * c;
+        *x = v < 0.0f ? 0.0f : v;
     }
 };
 struct EpiQuality {  // sum V*log10(WH+eps) - WH   (nmf_kernels_quality.cu:35)
@@ -298,18 +322,28 @@ cudaError_t gemm_f32(int M, int N, int K, F32Operand A, F32Operand B, float *C, 
     return gemm_store(M, N, K, LdCMT{A.p, A.ld}, LdCMT{B.p, B.ld}, C, ldc, splits, s);
 }
 
-cudaError_t gemm_f32_ratio_left(int M, int N, int K, const float *V, const float *WH, long long ldv,
-                                float eps, F32Operand B, float *P, int splits, cudaStream_t s) {
-    LdRatio ra{V, WH, ldv, eps};
+template <class LR>
+static cudaError_t ratio_left(int M, int N, int K, LR ra, F32Operand B, float *P, int splits, cudaStream_t s) {
     if (B.t) return gemm_store(M, N, K, ra, LdCMT{B.p, B.ld}, P, M, splits, s);
     return gemm_store(M, N, K, ra, LdCM{B.p, B.ld}, P, M, splits, s);
 }
 
-cudaError_t gemm_f32_ratio_right(int M, int N, int K, F32Operand A, const float *V, const float *WH,
-                                 long long ldv, float eps, float *P, int splits, cudaStream_t s) {
-    LdRatio rb{V, WH, ldv, eps};
+template <class LR>
+static cudaError_t ratio_right(int M, int N, int K, F32Operand A, LR rb, float *P, int splits, cudaStream_t s) {
     if (A.t) return gemm_store(M, N, K, LdCMT{A.p, A.ld}, rb, P, M, splits, s);
     return gemm_store(M, N, K, LdCM{A.p, A.ld}, rb, P, M, splits, s);
+}
+
+cudaError_t gemm_f32_ratio_left(int M, int N, int K, const float *V, const float *WH, long long ldv,
+                                float eps, F32Operand B, float *P, int splits, cudaStream_t s, bool minus_one) {
+    if (minus_one) return ratio_left(M, N, K, LdRatioM1{V, WH, ldv, eps}, B, P, splits, s);
+    return ratio_left(M, N, K, LdRatio{V, WH, ldv, eps}, B, P, splits, s);
+}
+
+cudaError_t gemm_f32_ratio_right(int M, int N, int K, F32Operand A, const float *V, const float *WH,
+                                 long long ldv, float eps, float *P, int splits, cudaStream_t s, bool minus_one) {
+    if (minus_one) return ratio_right(M, N, K, A, LdRatioM1{V, WH, ldv, eps}, P, splits, s);
+    return ratio_right(M, N, K, A, LdRatio{V, WH, ldv, eps}, P, splits, s);
 }
 
 int wh_reduce_ctas(int n, int m) {
@@ -344,6 +378,20 @@ cudaError_t kl_update_w_ref(float *W, const float *H, const float *V, const floa
     // acc(i,a) = sum_u [V(i,u)/(WH(i,u)+eps)] * H(a,u);  W(i,a) *= acc / sumH[a]
     EpiKLUpdate e{W, (long long)n, sumH, false};
     return launch_tiled(pick_tile(n, r), n, r, m, 1, LdRatio{V, WH, n, eps}, LdCMT{H, r}, e, s);
+}
+
+cudaError_t akl_update_h_ref(float *H, const float *W, const float *V, const float *WH,
+                             const float *sumW, int n, int m, int r, float eps, cudaStream_t s) {
+    // acc(a,u) = sum_i W(i,a) * [V(i,u)/(WH(i,u)+eps) - 1];  H(a,u) = max(0, h + (h/sumW[a]) acc)
+    EpiAKLUpdate e{H, (long long)r, sumW, true};
+    return launch_tiled(pick_tile(r, m), r, m, n, 1, LdCMT{W, n}, LdRatioM1{V, WH, n, eps}, e, s);
+}
+
+cudaError_t akl_update_w_ref(float *W, const float *H, const float *V, const float *WH,
+                             const float *sumH, int n, int m, int r, float eps, cudaStream_t s) {
+    // acc(i,a) = sum_u [V(i,u)/(WH(i,u)+eps) - 1] * H(a,u);  W(i,a) = max(0, w + (w/sumH[a]) acc)
+    EpiAKLUpdate e{W, (long long)n, sumH, false};
+    return launch_tiled(pick_tile(n, r), n, r, m, 1, LdRatioM1{V, WH, n, eps}, LdCMT{H, r}, e, s);
 }
 
 // ------------------------------------------------------------------------
@@ -433,6 +481,47 @@ cudaError_t euclid_update(float *X, const float *P, int splits, const float *D, 
     return cudaGetLastError();
 }
 
+// X = max(0, X + (X / D) * (num - D))   (nmf_kernels.cu:31-38; no epsilon, as there)
+__device__ __forceinline__ float additive_step(float x, float num, float d) {
+    float v = x + (x / d) * (num - d);
+    return v < 0.0f ? 0.0f : v;
+}
+
+__global__ void additive_update_kernel(float *__restrict__ X, const float *__restrict__ P, int splits,
+                                       const float *__restrict__ D, long long count) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride)
+        X[k] = additive_step(X[k], sum_slices(P, splits, count, k), D[k]);
+}
+
+__global__ void additive_update_kernel_v4(float4 *__restrict__ X, const float4 *__restrict__ P, int splits,
+                                          const float4 *__restrict__ D, long long count4) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count4; k += stride) {
+        float4 num = sum_slices4(P, splits, count4, k);
+        float4 d = D[k], x = X[k];
+        x.x = additive_step(x.x, num.x, d.x);
+        x.y = additive_step(x.y, num.y, d.y);
+        x.z = additive_step(x.z, num.z, d.z);
+        x.w = additive_step(x.w, num.w, d.w);
+        X[k] = x;
+    }
+}
+
+cudaError_t additive_update(float *X, const float *P, int splits, const float *D, long long count,
+                            cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    if ((count & 3) == 0 && aligned16(X) && aligned16(P) && aligned16(D)) {
+        long long c4 = count >> 2;
+        additive_update_kernel_v4<<<ew_blocks(c4, 2), kEwThreads, 0, s>>>(
+            reinterpret_cast<float4 *>(X), reinterpret_cast<const float4 *>(P), splits,
+            reinterpret_cast<const float4 *>(D), c4);
+    } else {
+        additive_update_kernel<<<ew_blocks(count), kEwThreads, 0, s>>>(X, P, splits, D, count);
+    }
+    return cudaGetLastError();
+}
+
 __global__ void sum_partials_kernel(float *__restrict__ out, const float *__restrict__ P, int splits,
                                     long long count) {
     long long stride = (long long)gridDim.x * blockDim.x;
@@ -457,10 +546,25 @@ __global__ void kl_update_kernel(float *__restrict__ X, const float *__restrict_
     }
 }
 
+__global__ void akl_update_kernel(float *__restrict__ X, const float *__restrict__ P, int splits,
+                                  const float *__restrict__ sums, long long count, long long div,
+                                  long long mod) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += stride) {
+        float acc = sum_slices(P, splits, count, k);
+        float x = X[k];
+        float v = x + (x / sums[(k / div) % mod]) * acc;
+        X[k] = v < 0.0f ? 0.0f : v;
+    }
+}
+
 cudaError_t kl_update(float *X, const float *P, int splits, const float *sums, long long count,
-                      long long div, long long mod, cudaStream_t s) {
+                      long long div, long long mod, cudaStream_t s, bool additive) {
     if (count <= 0) return cudaSuccess;
-    kl_update_kernel<<<ew_blocks(count), kEwThreads, 0, s>>>(X, P, splits, sums, count, div, mod);
+    if (additive)
+        akl_update_kernel<<<ew_blocks(count), kEwThreads, 0, s>>>(X, P, splits, sums, count, div, mod);
+    else
+        kl_update_kernel<<<ew_blocks(count), kEwThreads, 0, s>>>(X, P, splits, sums, count, div, mod);
     return cudaGetLastError();
 }
 

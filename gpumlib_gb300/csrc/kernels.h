@@ -20,12 +20,15 @@ struct F32Operand {
 cudaError_t gemm_f32(int M, int N, int K, F32Operand A, F32Operand B, float *C, long long ldc,
                      int splits, cudaStream_t s);
 
-// C = R op(B) or op(A) R where R = V / (WH + eps) is formed while loading
-// (the KL ratio, src/cuda/nmf/nmf_kernels.cu:271,319).  ratio_is_a selects the side.
+// C = R op(B) (left) or op(A) R (right) where R = V / (WH + eps) is formed while loading
+// (the KL ratio, src/cuda/nmf/nmf_kernels.cu:271,319); minus_one forms V / (WH + eps) - 1
+// instead (the additive KL rule, src/cuda/nmf/nmf_kernels_additive_divergence.cu:90,159).
 cudaError_t gemm_f32_ratio_left(int M, int N, int K, const float *V, const float *WH, long long ldv,
-                                float eps, F32Operand B, float *P, int splits, cudaStream_t s);
+                                float eps, F32Operand B, float *P, int splits, cudaStream_t s,
+                                bool minus_one = false);
 cudaError_t gemm_f32_ratio_right(int M, int N, int K, F32Operand A, const float *V, const float *WH,
-                                 long long ldv, float eps, float *P, int splits, cudaStream_t s);
+                                 long long ldv, float eps, float *P, int splits, cudaStream_t s,
+                                 bool minus_one = false);
 
 // Number of split-K slices gemm_f32* will use for this shape (so callers can size partials).
 int gemm_f32_splits(int M, int N, int K);
@@ -57,12 +60,18 @@ cudaError_t finalize_partials(const double *partial, int count, int terms, int m
 cudaError_t euclid_update(float *X, const float *P, int splits, const float *D, long long count,
                           float eps, cudaStream_t s);
 
+// X[k] = max(0, X[k] + (X[k] / D[k]) * (num - D[k])), num = sum_z P[z*count + k]
+// (the additive Euclidean update, nmf_kernels.cu:31-38; no epsilon, as there)
+cudaError_t additive_update(float *X, const float *P, int splits, const float *D, long long count,
+                            cudaStream_t s);
+
 // out[k] = sum_z P[z*count + k] (fixed order)
 cudaError_t sum_partials(float *out, const float *P, int splits, long long count, cudaStream_t s);
 
 // KL epilogue: X[k] *= (sum_z P[z*count+k]) / sums[(k / div) % mod]   (nmf_kernels.cu:289,337)
+// additive: X[k] = max(0, X[k] + (X[k] / sums[..]) * acc)   (nmf_kernels_additive_divergence.cu:101-104)
 cudaError_t kl_update(float *X, const float *P, int splits, const float *sums, long long count,
-                      long long div, long long mod, cudaStream_t s);
+                      long long div, long long mod, cudaStream_t s, bool additive = false);
 
 // sums[a] = max(sum_i W(i,a), eps) (KernelSumW, nmf_kernels.cu:63-147)
 cudaError_t col_sums(const float *W, int n, int r, float eps, float *sums, cudaStream_t s);
@@ -75,5 +84,10 @@ cudaError_t kl_update_h_ref(float *H, const float *W, const float *V, const floa
                             const float *sumW, int n, int m, int r, float eps, cudaStream_t s);
 cudaError_t kl_update_w_ref(float *W, const float *H, const float *V, const float *WH,
                             const float *sumH, int n, int m, int r, float eps, cudaStream_t s);
+// The same for the additive KL rule (nmf_kernels_additive_divergence.cu:39-185).
+cudaError_t akl_update_h_ref(float *H, const float *W, const float *V, const float *WH,
+                             const float *sumW, int n, int m, int r, float eps, cudaStream_t s);
+cudaError_t akl_update_w_ref(float *W, const float *H, const float *V, const float *WH,
+                             const float *sumH, int n, int m, int r, float eps, cudaStream_t s);
 
 }  // namespace gpunmf

@@ -340,7 +340,7 @@ gpunmf_status gpunmf_server_create(int slots, size_t hbm_budget_bytes, int preci
 
 gpunmf_status gpunmf_server_submit(gpunmf_server *S, long long id, int rule, int n, int m, int r,
                                    unsigned long long seed, float eps) {
-    if (!S || n <= 0 || m <= 0 || r <= 0 || (rule != GPUNMF_EUCLIDEAN && rule != GPUNMF_DIVERGENCE)) {
+    if (!S || n <= 0 || m <= 0 || r <= 0 || !rule_valid(rule)) {
         set_error("invalid job");
         return GPUNMF_ERR_INVALID;
     }

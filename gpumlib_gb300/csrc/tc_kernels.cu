@@ -307,7 +307,8 @@ __global__ void convert_h_kernel(const float *__restrict__ H, int r, int m, __nv
 }
 
 // ------------------------------------------------------------------------
-// update kernel (FP32): the multiplicative rule of nmf_kernels.cu:43-47 on an
+// update kernel (FP32): the multiplicative rule of nmf_kernels.cu:43-47 (or the
+// additive rule of nmf_kernels.cu:31-38) on an
 // r x 32 tile X of the factor being updated, with
 //   H-step: X = H(:, u0:u0+32),   den = G_W X          (G_W = W'W)
 //   W-step: X = W(i0:i0+32, :)',  den = G_H X = (X' G_H)'  (G_H = H H', symmetric)
@@ -334,6 +335,7 @@ struct UpdParams {
     int r, cols, npad;
     float eps;
     int update;               // 0: only write the Gram partials of X (initialisation)
+    int additive;             // 1: X = max(0, X + (X / den) (num - den)) (nmf_kernels.cu:31-38)
 };
 
 template <int RP, bool IS_W>
@@ -465,7 +467,14 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
             for (int j = 0; j < CPT; j++) {
                 int a = ga * TA + i;
                 float x = xv[i][j];
-                if (a < r) x *= nv[i][j] / (den[i][j] + p.eps);
+                if (a < r && gc * CPT + j < ncol) {  // outside stays 0 (the additive step has no eps)
+                    if (p.additive) {
+                        x = x + (x / den[i][j]) * (nv[i][j] - den[i][j]);
+                        x = x < 0.f ? 0.f : x;
+                    } else {
+                        x *= nv[i][j] / (den[i][j] + p.eps);
+                    }
+                }
                 Xn[(gc * CPT + j) * LDN + a] = x;
             }
     } else {
@@ -858,7 +867,9 @@ __global__ void __launch_bounds__(kKlThreads, 1)
 
 // KL update (nmf_kernels.cu:289,337 with the eps clamp of :104,190): X *= num / max(sum, eps)
 // on a 16-wide tile; writes X, its two BF16 copies, and this tile's partial sums over its columns
-// (the other half-step's denominator).
+// (the other half-step's denominator).  The additive KL rule
+// (nmf_kernels_additive_divergence.cu:90-104,159-173) needs sum_k f_k (R_k - 1) =
+// num - sum_k f_k: the same numerator less the unclamped sum of the other factor.
 struct KlUpdParams {
     float *X;
     __nv_bfloat16 *Xb;   // element (a, c) at a*ldb + c   (Hb row-major / Wb column-major)
@@ -873,13 +884,14 @@ struct KlUpdParams {
     int r, cols, npad;
     float eps;
     int update;
+    int additive;        // 1: X = max(0, X + (X / max(sum, eps)) (num - sum))
 };
 
 template <int RP, bool IS_W>
 __global__ void __launch_bounds__(kUpdThreads) tc_kl_update_kernel(KlUpdParams p) {
     constexpr int LDX = kUpdCols + 1;
     __shared__ float Xs[RP * LDX];
-    __shared__ float sumS[RP];
+    __shared__ float sumS[RP], sumR[RP];
     const int tid = threadIdx.x;
     const int c0 = blockIdx.x * kUpdCols;
     const int ncol = min(kUpdCols, p.cols - c0);
@@ -900,7 +912,11 @@ __global__ void __launch_bounds__(kUpdThreads) tc_kl_update_kernel(KlUpdParams p
         }
         acc[j] = 0.f;
     }
-    if (tid < RP) sumS[tid] = p.update ? fmaxf(p.sums[tid], p.eps) : 1.f;
+    if (tid < RP) {
+        const float sraw = p.update ? p.sums[tid] : 0.f;
+        sumS[tid] = p.update ? fmaxf(sraw, p.eps) : 1.f;
+        sumR[tid] = sraw;
+    }
     if (p.update) {
         const int tile = c0 / 128, lrow0 = c0 % 128;
         auto add_slot = [&](int sl) {
@@ -934,7 +950,12 @@ __global__ void __launch_bounds__(kUpdThreads) tc_kl_update_kernel(KlUpdParams p
         else      { c = k / RP; a = k % RP; }
         float x = xv[j];
         if (p.update && a < r && c < ncol) {
-            x *= (acc[j] / sumS[a]);
+            if (p.additive) {
+                x = x + (x / sumS[a]) * (acc[j] - sumR[a]);
+                x = x < 0.f ? 0.f : x;
+            } else {
+                x *= (acc[j] / sumS[a]);
+            }
             if (IS_W) p.X[(long long)a * p.ldx + c0 + c] = x;
             else p.X[(long long)(c0 + c) * r + a] = x;
         }
@@ -1216,6 +1237,7 @@ static UpdParams update_params_h(gpunmf_job *j, int update) {
     u.slot_ptr = t->gh.slot_ptr; u.slot_list = t->gh.slot_list; u.tile_slots = t->gh.tile_slots;
     u.gram_partials = t->GP_h;
     u.r = j->r; u.cols = j->m; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    u.additive = rule_is_additive(j->rule);
     return u;
 }
 
@@ -1226,6 +1248,7 @@ static UpdParams update_params_w(gpunmf_job *j, int update) {
     u.slot_ptr = t->gw.slot_ptr; u.slot_list = t->gw.slot_list; u.tile_slots = t->gw.tile_slots;
     u.gram_partials = t->GP_w;
     u.r = j->r; u.cols = j->n; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    u.additive = rule_is_additive(j->rule);
     return u;
 }
 
@@ -1343,6 +1366,7 @@ static KlUpdParams kl_params_h(gpunmf_job *j, int update) {
     u.slot_ptr = t->kh.slot_ptr; u.slot_list = t->kh.slot_list; u.tile_slots = t->kh.tile_slots;
     u.sum_partials = t->SP_h;
     u.r = j->r; u.cols = j->m; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    u.additive = rule_is_additive(j->rule);
     return u;
 }
 
@@ -1354,6 +1378,7 @@ static KlUpdParams kl_params_w(gpunmf_job *j, int update) {
     u.slot_ptr = t->kw.slot_ptr; u.slot_list = t->kw.slot_list; u.tile_slots = t->kw.tile_slots;
     u.sum_partials = t->SP_w;
     u.r = j->r; u.cols = j->n; u.npad = t->npad; u.eps = j->eps; u.update = update;
+    u.additive = rule_is_additive(j->rule);
     return u;
 }
 
@@ -1402,7 +1427,7 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
 gpunmf_status tc_supported(int rule, int n, int m, int r) {
     (void)n;
     (void)m;
-    if (rule == GPUNMF_DIVERGENCE) {
+    if (rule_is_kl(rule)) {
         if (r > kKlMaxRank) {
             set_error("BF16 KL path supports r <= %d", kKlMaxRank);
             return GPUNMF_ERR_UNSUPPORTED;
@@ -1420,7 +1445,7 @@ void tc_add_sizes(int, int, int, int, size_t *) {}
 
 size_t tc_footprint(int rule, int n, int m, int r) {
     const int npad = npad_of(r);
-    if (rule == GPUNMF_DIVERGENCE) {
+    if (rule_is_kl(rule)) {
         size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r +
                         (size_t)(n + m) * npad);
         b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
@@ -1443,7 +1468,7 @@ gpunmf_status tc_create(gpunmf_job *j) {
     t->ldvt = ceil8(m);
     t->ldw = ceil8(n);
     t->ldh = ceil8(m);
-    if (j->rule == GPUNMF_DIVERGENCE) return tc_create_kl(j);
+    if (rule_is_kl(j->rule)) return tc_create_kl(j);
     cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->ldv * m * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->ldvt * n * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
@@ -1502,7 +1527,7 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
     convert_h_kernel<<<std::min(1024, ceil_div((long long)j->r * j->m, 256)), 256, 0, s>>>(j->H, j->r, j->m,
                                                                                           t->Hb, t->ldh);
     GPUNMF_CUDA_TRY(cudaGetLastError());
-    if (j->rule == GPUNMF_DIVERGENCE) {
+    if (rule_is_kl(j->rule)) {
         convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->n * t->ldr, 256)), 256, 0, s>>>(
             j->W, j->n, j->r, j->n, true, t->Wr, t->ldr);
         convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->m * t->ldr, 256)), 256, 0, s>>>(
@@ -1514,6 +1539,9 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
     }
     // Gram partials of the initial W, finished by the first H-step GEMM
     GPUNMF_CUDA_TRY(launch_update(update_params_w(j, 0), t->npad, true, s));
+    // a rule without an H step: the Gram partials of the (fixed) H, finished by every W-step GEMM
+    if (j->rule == GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H)
+        GPUNMF_CUDA_TRY(launch_update(update_params_h(j, 0), t->npad, false, s));
     return GPUNMF_OK;
 }
 
@@ -1538,8 +1566,9 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
         gpunmf_status st = job_quality_step(j, true);
         if (st != GPUNMF_OK) return st;
     }
-    if (j->rule == GPUNMF_DIVERGENCE) {
+    if (rule_is_kl(j->rule)) {
         // H <- H .* [W'(V ./ (WH + eps))] ./ max(colsum W, eps); the kernel also finishes colsum W
+        // (additive KL: the same numerator, applied as H + (H / max(colsum W, eps)) (num - colsum W))
         mark_begin(j);
         GPUNMF_CUDA_TRY(launch_kl_gemm(t->kh, s));
         mark_end(j);
@@ -1554,12 +1583,14 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
         j->launches += 2;
         return GPUNMF_OK;
     }
-    // H <- H .* (W'V) ./ (W'W H + eps); the GEMM also finishes W'W
-    mark_begin(j);
-    GPUNMF_CUDA_TRY(launch_gemm(t->gh, s));
-    mark_end(j);
-    GPUNMF_CUDA_TRY(launch_update(update_params_h(j, 1), t->npad, false, s));
-    j->launches += 2;
+    // H <- H .* (W'V) ./ (W'W H + eps), or the additive step; the GEMM also finishes W'W
+    if (j->rule != GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H) {
+        mark_begin(j);
+        GPUNMF_CUDA_TRY(launch_gemm(t->gh, s));
+        mark_end(j);
+        GPUNMF_CUDA_TRY(launch_update(update_params_h(j, 1), t->npad, false, s));
+        j->launches += 2;
+    }
     if (!updateW) return GPUNMF_OK;
     // W <- W .* (V H') ./ (W H H' + eps); the GEMM also finishes H H'
     mark_begin(j);

@@ -2,8 +2,10 @@
 
 Same class names, constructor forms and methods as
 src/algorithms/nmf/nmf_base.h:45-151,
-src/algorithms/nmf/nmf_multiplicative_euclidian.h:51-65 and
-src/algorithms/nmf/nmf_multiplicative_divergence.h:48-58:
+src/algorithms/nmf/nmf_multiplicative_euclidian.h:51-65,
+src/algorithms/nmf/nmf_multiplicative_divergence.h:48-58,
+src/algorithms/nmf/nmf_additive_euclidian.h:35-67 and
+src/algorithms/nmf/nmf_additive_divergence.h:35-60:
 
     nmf = NMF_MultiplicativeEuclidianDistance(V, r)        # random W, H
     nmf = NMF_MultiplicativeEuclidianDistance(V, W, H)     # given W, H
@@ -25,6 +27,9 @@ from . import _native
 
 EUCLIDEAN = 0
 DIVERGENCE = 1
+ADDITIVE_EUCLIDEAN = 2
+ADDITIVE_DIVERGENCE = 3
+ADDITIVE_EUCLIDEAN_FIXED_H = 4
 PRECISIONS = {"fp32": 0, "bf16": 1}
 REFERENCE_EPS = np.float32(1e-8)
 
@@ -156,6 +161,39 @@ class NMF_MultiplicativeEuclidianDistance(NMF):
 class NMF_MultiplicativeDivergence(NMF):
     """Multiplicative updates, Kullback-Leibler divergence (nmf_multiplicative_divergence.h:35)."""
     _rule = DIVERGENCE
+
+
+class NMF_AdditiveEuclidian(NMF):
+    """Additive updates, Euclidean distance (nmf_additive_euclidian.h:35).
+
+    By default it runs exactly what the reference's GPU class runs: that class's
+    H step (nmf_additive_euclidian.cpp:37-42) passes (H, deltaH, deltaH2) to the
+    multiplicative kernel, which overwrites the deltaH2 workspace and leaves H
+    unchanged, so only W is updated.  ``update_h=True`` applies the additive
+    step to H as well, as the reference's CPU NMF does (HostNMF.h:152-190).
+    """
+
+    def __init__(self, v, r_or_w, h=None, *, update_h=False, **kw):
+        self._rule = ADDITIVE_EUCLIDEAN if update_h else ADDITIVE_EUCLIDEAN_FIXED_H
+        super().__init__(v, r_or_w, h, **kw)
+
+
+class NMF_AdditiveDivergence(NMF):
+    """Additive updates, Kullback-Leibler divergence (nmf_additive_divergence.h:35)."""
+    _rule = ADDITIVE_DIVERGENCE
+
+
+CLASSES = {EUCLIDEAN: NMF_MultiplicativeEuclidianDistance, DIVERGENCE: NMF_MultiplicativeDivergence,
+           ADDITIVE_DIVERGENCE: NMF_AdditiveDivergence}
+
+
+def make(rule, v, r_or_w, h=None, **kw):
+    """The class instance for a rule number (0..4, the gpunmf_rule values)."""
+    if rule == ADDITIVE_EUCLIDEAN:
+        return NMF_AdditiveEuclidian(v, r_or_w, h, update_h=True, **kw)
+    if rule == ADDITIVE_EUCLIDEAN_FIXED_H:
+        return NMF_AdditiveEuclidian(v, r_or_w, h, update_h=False, **kw)
+    return CLASSES[rule](v, r_or_w, h, **kw)
 
 
 def footprint_bytes(rule, n, m, r, precision="fp32"):

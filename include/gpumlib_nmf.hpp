@@ -5,6 +5,8 @@
  *   GPUMLib::NMF                                  src/algorithms/nmf/nmf_base.h:45-151
  *   GPUMLib::NMF_MultiplicativeEuclidianDistance  src/algorithms/nmf/nmf_multiplicative_euclidian.h:35-73
  *   GPUMLib::NMF_MultiplicativeDivergence         src/algorithms/nmf/nmf_multiplicative_divergence.h:35-63
+ *   GPUMLib::NMF_AdditiveEuclidian                src/algorithms/nmf/nmf_additive_euclidian.h:35-67
+ *   GPUMLib::NMF_AdditiveDivergence               src/algorithms/nmf/nmf_additive_divergence.h:35-60
  *   GPUMLib::HostMatrix<T> (the subset the NMF callers use)   src/memory/HostMatrix.h:37-132
  * implemented over the C ABI in gpunmf.h (link with -lgpunmf).
  *
@@ -187,6 +189,35 @@ class NMF_MultiplicativeDivergence : public NMF {
     NMF_MultiplicativeDivergence(HostMatrix<cudafloat> &v, HostMatrix<cudafloat> &w, HostMatrix<cudafloat> &h,
                                  float eps = GPUNMF_REFERENCE_EPS, int precision = GPUNMF_FP32)
         : NMF(GPUNMF_DIVERGENCE, v, w, h, eps, precision) {}
+    void DoIteration(bool updateW = true) override { nmf_check(gpunmf_iterate(h_, 1, updateW ? 1 : 0)); }
+};
+
+//! Additive update rules, Euclidean distance (nmf_additive_euclidian.h:35).  By default it runs
+//! what the reference's GPU class runs: that class's H step (nmf_additive_euclidian.cpp:37-42)
+//! overwrites a workspace instead of H, so H keeps its initial value and only W is updated.
+//! updateH = true applies the additive step to H as well (HostNMF.h:152-190).
+class NMF_AdditiveEuclidian : public NMF {
+  public:
+    NMF_AdditiveEuclidian(HostMatrix<cudafloat> &v, int r, bool updateH = false, int precision = GPUNMF_FP32,
+                          unsigned long long seed = 0)
+        : NMF(updateH ? GPUNMF_ADDITIVE_EUCLIDEAN : GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H, v, r,
+              GPUNMF_REFERENCE_EPS, precision, seed) {}
+    NMF_AdditiveEuclidian(HostMatrix<cudafloat> &v, HostMatrix<cudafloat> &w, HostMatrix<cudafloat> &h,
+                          bool updateH = false, int precision = GPUNMF_FP32)
+        : NMF(updateH ? GPUNMF_ADDITIVE_EUCLIDEAN : GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H, v, w, h,
+              GPUNMF_REFERENCE_EPS, precision) {}
+    void DoIteration(bool updateW = true) override { nmf_check(gpunmf_iterate(h_, 1, updateW ? 1 : 0)); }
+};
+
+//! Additive update rules, Kullback-Leibler divergence (nmf_additive_divergence.h:35).
+class NMF_AdditiveDivergence : public NMF {
+  public:
+    NMF_AdditiveDivergence(HostMatrix<cudafloat> &v, int r, float eps = GPUNMF_REFERENCE_EPS,
+                           int precision = GPUNMF_FP32, unsigned long long seed = 0)
+        : NMF(GPUNMF_ADDITIVE_DIVERGENCE, v, r, eps, precision, seed) {}
+    NMF_AdditiveDivergence(HostMatrix<cudafloat> &v, HostMatrix<cudafloat> &w, HostMatrix<cudafloat> &h,
+                           float eps = GPUNMF_REFERENCE_EPS, int precision = GPUNMF_FP32)
+        : NMF(GPUNMF_ADDITIVE_DIVERGENCE, v, w, h, eps, precision) {}
     void DoIteration(bool updateW = true) override { nmf_check(gpunmf_iterate(h_, 1, updateW ? 1 : 0)); }
 };
 

@@ -50,8 +50,17 @@ typedef enum {
 
 /* Update rules (GPUMLib class names in brackets). */
 typedef enum {
-    GPUNMF_EUCLIDEAN = 0,   /* NMF_MultiplicativeEuclidianDistance */
-    GPUNMF_DIVERGENCE = 1   /* NMF_MultiplicativeDivergence (KL)   */
+    GPUNMF_EUCLIDEAN = 0,            /* NMF_MultiplicativeEuclidianDistance              */
+    GPUNMF_DIVERGENCE = 1,           /* NMF_MultiplicativeDivergence (KL)                */
+    GPUNMF_ADDITIVE_EUCLIDEAN = 2,   /* additive Euclidean rule with both factors updated
+                                        (HostNMF::DoIteration_AE, HostNMF.h:152-190)      */
+    GPUNMF_ADDITIVE_DIVERGENCE = 3,  /* NMF_AdditiveDivergence (additive KL)             */
+    GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H = 4
+                                     /* NMF_AdditiveEuclidian exactly as the reference's GPU
+                                        class runs it: its H step hands (H, deltaH, deltaH2)
+                                        to the multiplicative kernel, which overwrites the
+                                        deltaH2 workspace, so H keeps its initial value
+                                        (nmf_additive_euclidian.cpp:37-42)                */
 } gpunmf_rule;
 
 /* Arithmetic of the factor products.  The W/H update itself is always FP32. */
@@ -267,6 +276,22 @@ int gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_w(
 
 /* nmf_kernels.h:113 — H(a,u) *= [sum_i W(i,a) V(i,u)/(WH(i,u)+1e-8)] / sumW[a] */
 int gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_h(
+    gpunmf_dim3 gridDim, gpunmf_dim3 blockDim, float *H, float *W, float *V, float *WH,
+    float *sumW, int n, int m, int r);
+
+/* nmf_kernels.h:116 — X[i] = max(0, X[i] + (X[i] / deltaX2[i]) * (deltaX1[i] - deltaX2[i])) */
+int gpumlib_cuda_nmf_additive_euclidean_update_matrix(
+    unsigned int gridDim, unsigned int blockDim, float *X, float *deltaX1, float *deltaX2, int elements);
+
+/* nmf_kernels.h:142 —
+   W(i,a) = max(0, W + (W / sumH[a]) * sum_u H(a,u) [V(i,u)/(WH(i,u)+1e-8) - 1]) */
+int gpumlib_cuda_nmf_additive_divergence_update_matrix_w(
+    gpunmf_dim3 gridDim, gpunmf_dim3 blockDim, float *W, float *H, float *V, float *WH,
+    float *sumH, int n, int m, int r);
+
+/* nmf_kernels.h:129 —
+   H(a,u) = max(0, H + (H / sumW[a]) * sum_i W(i,a) [V(i,u)/(WH(i,u)+1e-8) - 1]) */
+int gpumlib_cuda_nmf_additive_divergence_update_matrix_h(
     gpunmf_dim3 gridDim, gpunmf_dim3 blockDim, float *H, float *W, float *V, float *WH,
     float *sumW, int n, int m, int r);
 

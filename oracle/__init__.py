@@ -31,6 +31,8 @@ def orc():
         vp, i, f, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
         lib.orc_hostnmf_me_iter.argtypes = [i, i, i, vp, vp, vp, i, f, vp, i]
         lib.orc_hostnmf_md_iter.argtypes = [i, i, i, vp, vp, vp, i, f, i, vp, i]
+        lib.orc_hostnmf_ae_iter.argtypes = [i, i, i, vp, vp, vp, i, i, vp, i]
+        lib.orc_hostnmf_ad_iter.argtypes = [i, i, i, vp, vp, vp, i, f, i, vp, i]
         lib.orc_hostnmf_wh.argtypes = [i, i, i, vp, vp, vp, i]
         lib.orc_f64_me_iter.argtypes = [i, i, i, vp, vp, vp, i, d, vp, i]
         lib.orc_f64_md_iter.argtypes = [i, i, i, vp, vp, vp, i, d, vp, i]
@@ -67,13 +69,15 @@ def _f32(a):
 
 
 def hostnmf_run(rule, V, W, H, iters, updateW=True, eps=1e-8, clamp_sums=False, nthreads=1,
-                residuals=False):
-    """Float transcription of HostNMF (rule 0 Euclidean, 1 KL); returns (W, H[, resid])."""
+                residuals=False, skip_h=False):
+    """Float transcription of HostNMF; rule 0 multiplicative Euclidean, 1 multiplicative KL,
+    2 additive Euclidean (skip_h: the GPU class's H step that leaves H unchanged), 3 additive KL.
+    Returns (W, H[, resid])."""
     lib = orc()
     V = _f32(V); W = _f32(W); H = _f32(H)
     n, m = V.shape
     r = W.shape[1]
-    if rule == 0:
+    if rule in (0, 2):
         ws = np.empty(2 * r * m + r * r + 2 * n * r, dtype=np.float32)
     else:
         ws = np.empty(n * m, dtype=np.float32)
@@ -81,8 +85,13 @@ def hostnmf_run(rule, V, W, H, iters, updateW=True, eps=1e-8, clamp_sums=False, 
     for _ in range(iters):
         if rule == 0:
             lib.orc_hostnmf_me_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, _p(ws), nthreads)
-        else:
+        elif rule == 1:
             lib.orc_hostnmf_md_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, int(clamp_sums),
+                                    _p(ws), nthreads)
+        elif rule == 2:
+            lib.orc_hostnmf_ae_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), int(skip_h), _p(ws), nthreads)
+        else:
+            lib.orc_hostnmf_ad_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, int(clamp_sums),
                                     _p(ws), nthreads)
         if residuals:
             res.append(residual(V, W, H, nthreads))

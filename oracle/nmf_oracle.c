@@ -7,8 +7,8 @@
  *
  * Two families of functions:
  *
- *  orc_hostnmf_*  float transcriptions of the reference's CPU NMF
- *                 (src/examples/FacesNMF/HostNMF.h:64-150) with the exact
+ *  orc_hostnmf_*  float transcriptions of the reference's CPU NMF, all four
+ *                 rules (src/examples/FacesNMF/HostNMF.h:64-233) with the exact
  *                 operation order of its naive products
  *                 (src/examples/FacesNMF/Matrix.h:48-72): every dot product is
  *                 a sequential float accumulation from index 0.  Built with
@@ -182,6 +182,101 @@ void orc_hostnmf_md_iter(int n, int m, int r, const float *V, float *W, float *H
     if (!updateW) return;
     fmul(Wv, Hv, WH, n, m, r, nthreads);
     parallel_range((long)n * r, nthreads, md_w, &a);
+}
+
+/* ------------------------------------------------------------------ */
+/* HostNMF::DoIteration_AE (HostNMF.h:152-190): additive Euclidean     */
+/* ------------------------------------------------------------------ */
+struct fadd_arg { float *X; const float *d1, *d2; };
+static void fadd(long lo, long hi, void *p) {
+    struct fadd_arg *a = (struct fadd_arg *)p;
+    for (long k = lo; k < hi; k++) {
+        float x = a->X[k];
+        float d2 = a->d2[k];
+        float lr = x / d2;
+        x += lr * (a->d1[k] - d2);
+        a->X[k] = (x < 0.0f) ? 0.0f : x;
+    }
+}
+
+/* ws must hold 2*r*m + r*r + 2*n*r floats.  skip_h = 1 reproduces the GPU class
+ * NMF_AdditiveEuclidian (nmf_additive_euclidian.cpp:42), whose H step writes into a
+ * workspace instead of H, so H never changes. */
+void orc_hostnmf_ae_iter(int n, int m, int r, const float *V, float *W, float *H,
+                         int updateW, int skip_h, float *ws, int nthreads) {
+    float *WtV = ws, *WtWH = WtV + (size_t)r * m, *WtW = WtWH + (size_t)r * m;
+    float *VHt = WtW + (size_t)r * r, *WHHt = VHt + (size_t)n * r;
+    struct fview Wt = {W, n, 1}, Vv = {V, n, 0}, Hv = {H, r, 0}, Ht = {H, r, 1};
+    struct fview Wv = {W, n, 0};
+    if (!skip_h) {
+        fmul(Wt, Vv, WtV, r, m, n, nthreads);
+        fmul(Wt, Wv, WtW, r, r, n, nthreads);
+        struct fview WtWv = {WtW, r, 0};
+        fmul(WtWv, Hv, WtWH, r, m, r, nthreads);
+        struct fadd_arg uh = {H, WtV, WtWH};
+        parallel_range((long)r * m, nthreads, fadd, &uh);
+    }
+    if (!updateW) return;
+    fmul(Vv, Ht, VHt, n, r, m, nthreads);
+    float *HHt = WtW;
+    fmul(Hv, Ht, HHt, r, r, m, nthreads);
+    struct fview HHtv = {HHt, r, 0};
+    fmul(Wv, HHtv, WHHt, n, r, r, nthreads);
+    struct fadd_arg uw = {W, VHt, WHHt};
+    parallel_range((long)n * r, nthreads, fadd, &uw);
+}
+
+/* ------------------------------------------------------------------ */
+/* HostNMF::DoIteration_AD (HostNMF.h:192-233): additive KL            */
+/* clamp_sums=1 applies the GPU kernels' max(sum, eps) on the sums.    */
+/* ------------------------------------------------------------------ */
+static void ad_h(long lo, long hi, void *p) {
+    struct md_arg *a = (struct md_arg *)p;
+    for (long e = lo; e < hi; e++) {
+        long ai = e / a->m, u = e % a->m;
+        float sum = 0.0f, sumW = 0.0f;
+        for (long i = 0; i < a->n; i++) {
+            float w = a->W[IDX(i, ai, a->n)];
+            sum += w * a->V[IDX(i, u, a->n)] / (a->WH[IDX(i, u, a->n)] + a->eps) - w;
+            sumW += w;
+        }
+        if (a->clamp && sumW < a->eps) sumW = a->eps;
+        float h = a->H[IDX(ai, u, a->r)];
+        float lr = h / sumW;
+        h += lr * sum;
+        a->H[IDX(ai, u, a->r)] = (h < 0.0f) ? 0.0f : h;
+    }
+}
+
+static void ad_w(long lo, long hi, void *p) {
+    struct md_arg *a = (struct md_arg *)p;
+    for (long e = lo; e < hi; e++) {
+        long i = e / a->r, ai = e % a->r;
+        float sum = 0.0f, sumH = 0.0f;
+        for (long u = 0; u < a->m; u++) {
+            float h = a->H[IDX(ai, u, a->r)];
+            sum += h * a->V[IDX(i, u, a->n)] / (a->WH[IDX(i, u, a->n)] + a->eps) - h;
+            sumH += h;
+        }
+        if (a->clamp && sumH < a->eps) sumH = a->eps;
+        float w = a->W[IDX(i, ai, a->n)];
+        float lr = w / sumH;
+        w += lr * sum;
+        a->W[IDX(i, ai, a->n)] = (w < 0.0f) ? 0.0f : w;
+    }
+}
+
+/* ws must hold n*m floats (WH) */
+void orc_hostnmf_ad_iter(int n, int m, int r, const float *V, float *W, float *H,
+                         int updateW, float eps, int clamp_sums, float *ws, int nthreads) {
+    struct fview Wv = {W, n, 0}, Hv = {H, r, 0};
+    float *WH = ws;
+    fmul(Wv, Hv, WH, n, m, r, nthreads);
+    struct md_arg a = {n, m, r, V, WH, W, H, eps, clamp_sums};
+    parallel_range((long)r * m, nthreads, ad_h, &a);
+    if (!updateW) return;
+    fmul(Wv, Hv, WH, n, m, r, nthreads);
+    parallel_range((long)n * r, nthreads, ad_w, &a);
 }
 
 /* W*H in Matrix::Multiply order (the WH that GetWH returns on the CPU) */

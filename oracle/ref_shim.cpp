@@ -31,19 +31,21 @@ static double rel_residual(int n, int m, int r, const float *V, const float *W, 
     return den > 0.0 ? std::sqrt(num / den) : 0.0;
 }
 
-// method: 0 multiplicative Euclidean, 1 multiplicative divergence
-// (HostNMF.h:32-37).  V (n x m), W (n x r), H (r x m) column-major.  W and H
+// method: 0 multiplicative Euclidean, 1 multiplicative divergence,
+// 2 additive Euclidean, 3 additive divergence (HostNMF.h:32-37).  V (n x m), W (n x r), H (r x m) column-major.  W and H
 // are inputs and outputs.  resid (nullable) receives the relative Frobenius
 // residual after every iteration.
 extern "C" int ref_hostnmf_run(int method, int n, int m, int r, const float *V, float *W, float *H,
                                int iters, int updateW, double *resid) {
-    if (method != 0 && method != 1) return -1;
+    if (method < 0 || method > 3) return -1;
+    static const NMF_METHOD methods[4] = {MULTIPLICATIVE_EUCLIDEAN, MULTIPLICATIVE_DIVERGENCE, ADDITIVE_EUCLIDEAN,
+                                          ADDITIVE_DIVERGENCE};
     HostNMF h(n, m, r);
     std::memcpy(h.V.Pointer(), V, sizeof(float) * (size_t)n * m);
     std::memcpy(h.W.Pointer(), W, sizeof(float) * (size_t)n * r);
     std::memcpy(h.H.Pointer(), H, sizeof(float) * (size_t)r * m);
     for (int it = 0; it < iters; it++) {
-        h.DoIteration(method == 0 ? MULTIPLICATIVE_EUCLIDEAN : MULTIPLICATIVE_DIVERGENCE, updateW != 0);
+        h.DoIteration(methods[method], updateW != 0);
         if (resid) resid[it] = rel_residual(n, m, r, V, h.W.Pointer(), h.H.Pointer());
     }
     std::memcpy(W, h.W.Pointer(), sizeof(float) * (size_t)n * r);

@@ -39,6 +39,13 @@ CASES = [
     ("kl_noW_40x30_r3", 1, 40, 30, 3, 10, False, 25, 26, {}),
     ("kl_sparse_48x40_r4", 1, 48, 40, 4, 10, True, 27, 28, {"sparse": 7}),
     ("kl_wide_20x160_r6", 1, 20, 160, 6, 12, True, 29, 30, {}),
+    # additive rules (HostNMF.h:152-233)
+    ("ae_200x150_r6", 2, 200, 150, 6, 15, True, 31, 32, {}),
+    ("ae_odd_37x23_r3", 2, 37, 23, 3, 10, True, 33, 34, {}),
+    ("ae_noW_50x40_r4", 2, 50, 40, 4, 8, False, 35, 36, {}),
+    ("ad_256x128_r8", 3, 256, 128, 8, 15, True, 37, 38, {}),
+    ("ad_odd_33x17_r5", 3, 33, 17, 5, 10, True, 39, 40, {}),
+    ("ad_noW_40x30_r3", 3, 40, 30, 3, 8, False, 41, 42, {}),
 ]
 
 

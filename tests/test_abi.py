@@ -1,7 +1,8 @@
 """The C ABI library loads and exports every function the public headers declare.
 
-No compute call is made here (the CPU suite runs without a GPU); create-type
-calls are only checked for their error status when no device is visible.
+No compute call is made by the CPU tests here; create-type calls are only
+checked for their error status when no device is visible.  The one GPU test
+runs the compiled C++ drop-in caller.
 """
 import ctypes
 import os
@@ -107,6 +108,27 @@ def test_cpp_dropin_header_compiles(built, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+@pytest.mark.gpu
+def test_cpp_dropin_caller_runs(built, tmp_path):
+    """The same caller runs on the GPU; the reference-form additive Euclidean class leaves H as given."""
+    from gpumlib_gb300 import _native
+    src = tmp_path / "caller.cpp"
+    src.write_text(CPP_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_native.lib_path())
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    r = subprocess.run(["g++", "-std=c++14", "-O1", "-I", os.path.join(ROOT, "include"), "-I", cuda + "/include",
+                        str(src), "-o", str(exe), "-L", libdir, "-lgpunmf", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+    lines = run.stdout.split("\n")
+    ae_h, ae2_h, ad_w = (float(x) for x in lines[2].split())
+    assert ae_h == np.float32(0.5), "fixed-H additive class changed H"
+    assert ae2_h != np.float32(0.5) and ae2_h >= 0 and ad_w >= 0
+
+
 CPP_CALLER = r"""
 #include <cstdio>
 #include "gpumlib_nmf.hpp"
@@ -127,6 +149,11 @@ int main() {
         kl.DoIteration(true); kl.DoIteration(false);
         HostMatrix<cudafloat> kw = kl.GetW();
         std::printf("%.9g\n", kw(1, 1));
+        NMF_AdditiveEuclidian ae(V, W, H);          // the reference GPU class: H stays as given
+        NMF_AdditiveEuclidian ae2(V, W, H, true);   // H updated as well
+        NMF_AdditiveDivergence ad(V, W, H);
+        ae.DoIteration(); ae2.DoIteration(); ad.DoIteration();
+        std::printf("%.9g %.9g %.9g\n", ae.GetH()(0, 0), ae2.GetH()(0, 0), ad.GetW()(0, 0));
     } catch (NMFError & e) {
         std::printf("error %d %s\n", (int)e.status, e.what());
         return 2;

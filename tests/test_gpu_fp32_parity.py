@@ -21,8 +21,8 @@ TOL_FACTOR = 1e-4
 
 
 def run_gpu(g, rule, V, W, H, iters, updateW=True, eps=1e-8, precision="fp32", **kw):
-    cls = g.NMF_MultiplicativeEuclidianDistance if rule == 0 else g.NMF_MultiplicativeDivergence
-    with cls(V, W, H, eps=eps, precision=precision, **kw) as nmf:
+    """Rule numbers as in gpunmf_rule: 0/1 multiplicative, 2/3 additive (both factors), 4 fixed-H."""
+    with g.make(rule, V, W, H, eps=eps, precision=precision, **kw) as nmf:
         nmf.Iterate(iters, updateW)
         return nmf.GetW(), nmf.GetH(), nmf.Residual()
 

@@ -36,10 +36,25 @@ def test_oracle_thread_count_invariant():
     from gpumlib_gb300 import inputs
     V = inputs.uniform_matrix(5, 70, 45)
     W, H = inputs.factors(6, 70, 45, 4)
-    for rule in (0, 1):
+    for rule in (0, 1, 2, 3):
         a = oracle.hostnmf_run(rule, V, W, H, 5, nthreads=1)
         b = oracle.hostnmf_run(rule, V, W, H, 5, nthreads=7)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_oracle_fixed_h_additive():
+    """skip_h reproduces the reference GPU class's additive Euclidean H step, which leaves H as it
+    was (nmf_additive_euclidian.cpp:37-42); its W step is HostNMF's (HostNMF.h:176-189)."""
+    from gpumlib_gb300 import inputs
+    V = inputs.uniform_matrix(7, 60, 40)
+    W, H = inputs.factors(8, 60, 40, 5)
+    Wf, Hf = oracle.hostnmf_run(2, V, W, H, 3, skip_h=True)
+    assert np.array_equal(Hf, H)
+    # one W step from the same H equals the full rule's W step when H is not updated first
+    W1, H1 = oracle.hostnmf_run(2, V, W, H, 1, skip_h=True)
+    Wd, Hd = W.astype(np.float64), H.astype(np.float64)
+    exp = np.maximum(Wd + Wd / (Wd @ (Hd @ Hd.T)) * (V @ Hd.T - Wd @ (Hd @ Hd.T)), 0)
+    assert np.linalg.norm(W1 - exp) / np.linalg.norm(exp) < 1e-5
 
 
 def test_f64_oracle_close_to_float_reference(golden):
