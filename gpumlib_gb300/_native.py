@@ -76,6 +76,9 @@ SIGNATURES = [
                                            ctypes.POINTER(ctypes.c_size_t)]),
     ("gpunmf_server_clock", ctypes.c_double, [ctypes.c_void_p]),
     ("gpunmf_server_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gpunmf_grouped_train", ctypes.c_int,
+     [ctypes.c_int] * 5 + [ctypes.c_void_p] * 3 + [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                                    ctypes.c_void_p]),
     ("gpumlib_cuda_nmf_multiplicative_euclidean_update_matrix", ctypes.c_int,
      [ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_w", ctypes.c_int,

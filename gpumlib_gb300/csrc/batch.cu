@@ -1,5 +1,6 @@
 // Batched multiplicative-update NMF: thousands of small, uneven Euclidean
-// factorisations in one persistent launch.
+// factorisations in one persistent launch, and FacesNMF's grouped training on
+// top of it (end of file).
 //
 // The reference's nearest equivalent is FacesNMF's grouped training
 // (src/examples/FacesNMF/FacesNMFDlg.cpp:582-656), which builds one NMF
@@ -26,6 +27,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "engine.h"
 #include "kernels.h"
 
 namespace gpunmf {
@@ -36,6 +38,12 @@ struct BatchInst {
 };
 
 constexpr int kBatchThreads = 256;
+
+// per-instance convergence test (grouped training)
+struct BatchStop {
+    float tol;
+    int *iterations;  // [instances] iterations run
+};
 constexpr int kBatchSmemFloats = 12288;  // 48 KB
 
 // 4-byte asynchronous global -> shared copy; zero-fills when !valid (src is then not read)
@@ -106,8 +114,60 @@ struct InstanceRunner {
         __syncthreads();
     }
 
+    // quality of the current factors, sum V log10(WH + eps) - WH (nmf_kernels_quality.cu:35), as the
+    // float the reference reads back; WH is formed tile by tile and never stored.  Same value on
+    // every thread.  Uses the V, factor and chunk areas of shared memory, not the Gram.
+    __device__ __noinline__ static float quality(const float *__restrict__ V, const float *__restrict__ W,
+                                    const float *__restrict__ H, int n, int m, int r, float eps, float *sm) {
+        __shared__ double qred[32];
+        float *sV = sm + OFF_V, *sF = sm + OFF_F, *sX = sm + OFF_X;
+        const int tid = threadIdx.x;
+        constexpr int EPT = BI * BC / kBatchThreads;  // tile elements per thread
+        static_assert(EPT * kBatchThreads == BI * BC, "tile/threads");
+        double t = 0.0;
+        for (int c0 = 0; c0 < m; c0 += BC) {
+            const int nc = min(BC, m - c0);
+            for (int k = tid; k < R * BC; k += kBatchThreads) {
+                const int u = k / R, a = k % R;
+                const bool ok = a < r && u < nc;
+                cp_async_f32(&sX[a * (BC + 4) + u], ok ? H + (long long)(c0 + u) * r + a : H, ok);
+            }
+            for (int i0 = 0; i0 < n; i0 += BI) {
+                const int nr = min(BI, n - i0);
+                for (int k = tid; k < BI * BC; k += kBatchThreads) {
+                    const int u = k / BI, ii = k % BI;
+                    const bool ok = ii < nr && u < nc;
+                    cp_async_f32(&sV[ii * (BC + 4) + u], ok ? V + (long long)(c0 + u) * n + i0 + ii : V, ok);
+                }
+                for (int k = tid; k < BI * R; k += kBatchThreads) {
+                    const int a = k / BI, ii = k % BI;
+                    const bool ok = a < r && ii < nr;
+                    cp_async_f32(&sF[ii * (R + 4) + a], ok ? W + (long long)a * n + i0 + ii : W, ok);
+                }
+                cp_async_wait_all();
+                __syncthreads();
+                float part = 0.f;
+#pragma unroll 4
+                for (int e = 0; e < EPT; e++) {
+                    const int q = tid + e * kBatchThreads, ii = q / BC, u = q % BC;
+                    float wh = 0.f;
+#pragma unroll
+                    for (int a = 0; a < R; a++) wh = fmaf(sF[ii * (R + 4) + a], sX[a * (BC + 4) + u], wh);
+                    if (ii < nr && u < nc) part += sV[ii * (BC + 4) + u] * log10f(wh + eps) - wh;
+                }
+                t += (double)part;
+                __syncthreads();
+            }
+        }
+        return (float)block_sum(t, qred);
+    }
+
+    // kStop: the convergence test of FacesNMF's grouped training (FacesNMFDlg.cpp:605-629) on the
+    // lagged quality improvement of nmf_base.h:70-89; without it exactly `iters` iterations run.
+    template <bool kStop>
     __device__ __noinline__ static void run(const BatchInst &d, const float *__restrict__ Vall, float *__restrict__ Wall,
-                               float *__restrict__ Hall, float eps, int iters, float *sm) {
+                               float *__restrict__ Hall, float eps, int iters, float *sm,
+                               const BatchStop &stop, int inst) {
         const int n = d.n, m = d.m, r = d.r;
         const float *V = Vall + d.v;
         float *W = Wall + d.w;
@@ -118,7 +178,32 @@ struct InstanceRunner {
 
         gram_init(sG, W, n, n, r, true, sF);  // G = W'W
 
+        // lag state exactly as the host engine keeps it, held by thread 0 in shared memory; the
+        // stop decision is taken when the iteration starts (the improvement it reports is known
+        // then) and read by every thread after the iteration's last barrier
+        struct Lag {
+            float value, last, delta, prev;
+            int times, stop_after;
+        };
+        __shared__ Lag lag;
+        if (kStop && tid == 0) lag = Lag{0.f, -1.f, 1.f, 1.f, 0, 0};
+        int done = iters;
         for (int it = 0; it < iters; it++) {
+            if constexpr (kStop) {
+                const float q_new = quality(V, W, H, n, m, r, eps, sm);  // contains barriers
+                if (tid == 0) {
+                    const float q_now = lag.value;
+                    if (lag.times++ > 2) lag.delta = q_now - lag.last;
+                    else lag.times++;
+                    lag.last = q_now;
+                    lag.value = q_new;
+                    lag.stop_after = 0;
+                    if (lag.delta != lag.prev) {
+                        if (lag.delta < stop.tol) lag.stop_after = 1;
+                        else lag.prev = lag.delta;
+                    }
+                }
+            }
             // ================= H-step =================
             float gacc[GE];
 #pragma unroll
@@ -294,7 +379,12 @@ struct InstanceRunner {
                 if (q < R * R) sG[q] = gacc[e];
             }
             __syncthreads();
+            if (kStop && lag.stop_after) {
+                done = it + 1;
+                break;
+            }
         }
+        if (kStop && tid == 0) stop.iterations[inst] = done;
     }
 };
 
@@ -314,10 +404,11 @@ __host__ __device__ constexpr int batch_cfg_rank(int c) {
     return c == 0 ? 4 : c == 1 ? 8 : c == 2 ? 16 : c == 3 ? 32 : c == 4 ? 8 : c == 5 ? 16 : c == 6 ? 32 : 4;  // config 7: rank 4
 }
 
+template <bool kStop>
 __global__ void __launch_bounds__(kBatchThreads, 3)
     batch_kernel(const BatchInst *__restrict__ insts, const int *__restrict__ order, int count,
                  int *__restrict__ next, const float *__restrict__ V, float *__restrict__ W, float *__restrict__ H,
-                 float eps, int iters) {
+                 float eps, int iters, BatchStop stop) {
     extern __shared__ float bsm[];
     __shared__ int s_idx;
     for (;;) {
@@ -329,7 +420,7 @@ __global__ void __launch_bounds__(kBatchThreads, 3)
         const BatchInst d = insts[order[k]];
         switch (d.cfg) {
 #define X(C, R, BC, BI) \
-    case C: InstanceRunner<R, BC, BI>::run(d, V, W, H, eps, iters, bsm); break;
+    case C: InstanceRunner<R, BC, BI>::template run<kStop>(d, V, W, H, eps, iters, bsm, stop, order[k]); break;
             GPUNMF_BATCH_CONFIGS(X)
 #undef X
             default: break;
@@ -448,9 +539,9 @@ static gpunmf_status batch_upload_order(gpunmf_batch *b) {
 
 static gpunmf_status batch_launch(gpunmf_batch *b, int iters) {
     GPUNMF_CUDA_TRY(cudaMemsetAsync(b->d_next, 0, sizeof(int), b->stream));
-    batch_kernel<<<b->grid, kBatchThreads, batch_max_smem(), b->stream>>>(b->d_insts, b->d_order, b->count,
+    batch_kernel<false><<<b->grid, kBatchThreads, batch_max_smem(), b->stream>>>(b->d_insts, b->d_order, b->count,
                                                                           b->d_next, b->V, b->W, b->H, b->eps,
-                                                                          iters);
+                                                                          iters, BatchStop{0.f, nullptr});
     GPUNMF_CUDA_TRY(cudaGetLastError());
     return GPUNMF_OK;
 }
@@ -497,7 +588,7 @@ gpunmf_status gpunmf_batch_create(int count, const int *n, const int *m, const i
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->W, sizeof(float) * b->w_total);
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->H, sizeof(float) * b->h_total);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_max_smem());
+        e = cudaFuncSetAttribute(batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_max_smem());
     if (e != cudaSuccess) {
         set_error("batch allocation failed: %s", cudaGetErrorString(e));
         cudaGetLastError();
@@ -534,7 +625,7 @@ gpunmf_status gpunmf_batch_create(int count, const int *n, const int *m, const i
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kBatchThreads, batch_max_smem());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<false>, kBatchThreads, batch_max_smem());
     b->grid = std::max(1, sms * std::max(1, per_sm));
     gpunmf_status st = batch_upload_order(b);
     if (st != GPUNMF_OK) {
@@ -664,3 +755,234 @@ gpunmf_status gpunmf_batch_reset_factors(gpunmf_batch *b, const float *const *W,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Grouped training (src/examples/FacesNMF/FacesNMFDlg.cpp:582-656, TrainUsingGroups).
+//
+// V's first blocks*group columns are cut into `blocks` = floor(m/group) blocks of `group`
+// consecutive columns; block s is an independent NMF of rank rs = floor(r/blocks).  Column
+// blocks of a column-major matrix are contiguous, so the blocks of V and W need no packing; the
+// diagonal blocks of H are gathered into a packed array and scattered back (zeros elsewhere in
+// the block's columns, as :640-651 writes).  Two ways to run the blocks:
+//   - multiplicative Euclidean, FP32, rs <= 32: every block is one instance of the persistent
+//     batch kernel above, which samples the quality itself and stops the instance on the
+//     reference's test (one launch for all blocks);
+//   - any other rule or precision: one engine job per block (the same code as the class API),
+//     up to 64 in flight on their own streams, driven round-robin by this thread; each job's
+//     quality read-back is one iteration behind, so the host rarely waits.
+// ---------------------------------------------------------------------------
+namespace gpunmf {
+
+__global__ void gather_h_blocks(const float *__restrict__ H, int r, int group, int rs, int blocks,
+                                float *__restrict__ Hp) {
+    const long long total = (long long)blocks * rs * group;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long s = k / ((long long)rs * group), rem = k % ((long long)rs * group);
+        const long long u = rem / rs, a = rem % rs;  // packed block: rs x group column-major
+        Hp[k] = H[(s * group + u) * r + s * rs + a];
+    }
+}
+
+__global__ void scatter_h_blocks(float *__restrict__ H, int r, int group, int rs, int blocks,
+                                 const float *__restrict__ Hp) {
+    const long long total = (long long)blocks * group * r;  // the first blocks*group columns of H
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long col = k / r, row = k % r;
+        const long long s = col / group, u = col % group, a = row - s * rs;
+        H[k] = (a >= 0 && a < rs) ? Hp[s * rs * group + u * rs + a] : 0.f;
+    }
+}
+
+static int ew_grid(long long count) {
+    long long b = (count + 255) / 256;
+    return (int)std::max(1LL, std::min(b, 8LL * kNumSMsGB300));
+}
+
+// one engine job per block, round-robin
+static gpunmf_status grouped_jobs(int rule, int n, int group, int rs, int blocks, const float *dV, float *dW,
+                                  float *dHp, float tol, int max_iters, float eps, int precision, int *iters_out) {
+    struct Slot {
+        gpunmf_job *j = nullptr;
+        int s = -1, its = 0;
+        float prev = 1.f;
+    };
+    const int window = std::min(blocks, 64);
+    std::vector<Slot> slots(window);
+    int next = 0, remaining = blocks;
+    gpunmf_status st = GPUNMF_OK;
+    const size_t vb = (size_t)n * group, wb = (size_t)n * rs, hb = (size_t)rs * group;
+    auto start = [&](Slot &sl) -> gpunmf_status {
+        sl.s = next++;
+        sl.its = 0;
+        gpunmf_status s2 = job_create_empty(rule, n, group, rs, eps, precision, nullptr, nullptr, false, &sl.j);
+        if (s2 != GPUNMF_OK) return s2;
+        cudaStream_t js = sl.j->stream;
+        GPUNMF_CUDA_TRY(cudaMemcpyAsync(sl.j->V, dV + sl.s * vb, vb * sizeof(float), cudaMemcpyDeviceToDevice, js));
+        GPUNMF_CUDA_TRY(cudaMemcpyAsync(sl.j->W, dW + sl.s * wb, wb * sizeof(float), cudaMemcpyDeviceToDevice, js));
+        GPUNMF_CUDA_TRY(cudaMemcpyAsync(sl.j->H, dHp + sl.s * hb, hb * sizeof(float), cudaMemcpyDeviceToDevice, js));
+        s2 = job_prepare(sl.j);
+        sl.prev = sl.j->q_delta;  // QualityImprovement() of a new object (FacesNMFDlg.cpp:605)
+        return s2;
+    };
+    auto finish = [&](Slot &sl) -> gpunmf_status {
+        cudaStream_t js = sl.j->stream;
+        GPUNMF_CUDA_TRY(cudaMemcpyAsync(dW + sl.s * wb, sl.j->W, wb * sizeof(float), cudaMemcpyDeviceToDevice, js));
+        GPUNMF_CUDA_TRY(cudaMemcpyAsync(dHp + sl.s * hb, sl.j->H, hb * sizeof(float), cudaMemcpyDeviceToDevice, js));
+        GPUNMF_CUDA_TRY(cudaStreamSynchronize(js));
+        iters_out[sl.s] = sl.its;
+        job_release(sl.j);
+        sl.j = nullptr;
+        remaining--;
+        return GPUNMF_OK;
+    };
+    while (st == GPUNMF_OK && remaining > 0) {
+        for (Slot &sl : slots) {
+            if (!sl.j) {
+                if (next >= blocks) continue;
+                st = start(sl);
+                if (st != GPUNMF_OK) break;
+            }
+            st = job_run(sl.j, 1, true);  // DoIteration(true) (FacesNMFDlg.cpp:610)
+            if (st != GPUNMF_OK) break;
+            sl.its++;
+            bool done = sl.its >= max_iters;
+            const float q = sl.j->q_delta;  // QualityImprovement() (:612-616)
+            if (q != sl.prev) {
+                if (q < tol) done = true;
+                else sl.prev = q;
+            }
+            if (done) {
+                st = finish(sl);
+                if (st != GPUNMF_OK) break;
+            }
+        }
+    }
+    for (Slot &sl : slots)
+        if (sl.j) job_release(sl.j);
+    return st;
+}
+
+}  // namespace gpunmf
+
+extern "C" gpunmf_status gpunmf_grouped_train(int rule, int n, int m, int r, int group, const float *V, float *W,
+                                              float *H, float tol, int max_iters, float eps, int precision,
+                                              int *iterations) {
+    if (!V || !W || !H || n <= 0 || m <= 0 || r <= 0 || group <= 0 || max_iters <= 0 || !rule_valid(rule) ||
+        !(eps >= 0.f) || (precision != GPUNMF_FP32 && precision != GPUNMF_BF16)) {
+        set_error("invalid grouped-training arguments");
+        return GPUNMF_ERR_INVALID;
+    }
+    const int blocks = m / group;
+    const int rs = blocks > 0 ? r / blocks : 0;
+    if (blocks < 1 || rs < 1) {
+        set_error("grouped training needs group <= m and r >= m/group (group %d, m %d, r %d)", group, m, r);
+        return GPUNMF_ERR_INVALID;
+    }
+    int devs = 0;
+    if (cudaGetDeviceCount(&devs) != cudaSuccess || devs == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device available");
+        return GPUNMF_ERR_NO_DEVICE;
+    }
+    const bool batched = rule == GPUNMF_EUCLIDEAN && precision == GPUNMF_FP32 && rank_class(rs) != 0;
+    const size_t vcount = (size_t)n * blocks * group, wcount = (size_t)n * blocks * rs, hcount = (size_t)r * m;
+    const size_t hpcount = (size_t)blocks * rs * group;
+    cudaStream_t s = nullptr;
+    float *dV = nullptr, *dW = nullptr, *dH = nullptr, *dHp = nullptr;
+    int *d_iters = nullptr, *d_order = nullptr, *d_next = nullptr;
+    BatchInst *d_insts = nullptr;
+    std::vector<int> h_iters(blocks, 0);
+    gpunmf_status st = GPUNMF_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&dV, vcount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&dW, wcount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&dH, hcount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&dHp, hpcount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_iters, blocks * sizeof(int));
+    if (e != cudaSuccess) {
+        set_error("grouped training allocation failed: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        st = GPUNMF_ERR_NOMEM;
+    }
+    // the blocks' V and W columns and the whole H (the columns outside the blocks come back as they were)
+    if (st == GPUNMF_OK) {
+        e = cudaMemcpyAsync(dV, V, vcount * sizeof(float), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dW, W, wcount * sizeof(float), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dH, H, hcount * sizeof(float), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) {
+            gather_h_blocks<<<ew_grid(hpcount), 256, 0, s>>>(dH, r, group, rs, blocks, dHp);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("grouped training upload failed: %s", cudaGetErrorString(e));
+            st = GPUNMF_ERR_CUDA;
+        }
+    }
+    if (st == GPUNMF_OK && batched) {
+        std::vector<BatchInst> insts(blocks);
+        std::vector<int> order(blocks);
+        for (int b = 0; b < blocks; b++) {
+            BatchInst &d = insts[b];
+            d.n = n; d.m = group; d.r = rs; d.cfg = default_cfg(rs);
+            d.v = (long long)b * n * group;
+            d.w = (long long)b * n * rs;
+            d.h = (long long)b * rs * group;
+            order[b] = b;
+        }
+        e = cudaMalloc((void **)&d_insts, blocks * sizeof(BatchInst));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d_order, blocks * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d_next, sizeof(int));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_insts, insts.data(), blocks * sizeof(BatchInst), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_order, order.data(), blocks * sizeof(int), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_next, 0, sizeof(int), s);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)batch_max_smem());
+        int dev = 0, sms = 0, per_sm = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<true>, kBatchThreads,
+                                                              batch_max_smem());
+        if (e == cudaSuccess) {
+            const int grid = std::max(1, std::min(blocks, sms * std::max(1, per_sm)));
+            batch_kernel<true><<<grid, kBatchThreads, batch_max_smem(), s>>>(d_insts, d_order, blocks, d_next, dV, dW,
+                                                                             dHp, eps, max_iters,
+                                                                             BatchStop{tol, d_iters});
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h_iters.data(), d_iters, blocks * sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) {
+            set_error("grouped batch launch failed: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            st = GPUNMF_ERR_CUDA;
+        }
+    } else if (st == GPUNMF_OK) {
+        st = grouped_jobs(rule, n, group, rs, blocks, dV, dW, dHp, tol, max_iters, eps, precision, h_iters.data());
+    }
+    if (st == GPUNMF_OK) {
+        scatter_h_blocks<<<ew_grid((long long)blocks * group * r), 256, 0, s>>>(dH, r, group, rs, blocks, dHp);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(W, dW, wcount * sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(H, dH, hcount * sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("grouped training read-back failed: %s", cudaGetErrorString(e));
+            st = GPUNMF_ERR_CUDA;
+        } else if (iterations) {
+            std::copy(h_iters.begin(), h_iters.end(), iterations);
+        }
+    }
+    if (s) cudaStreamSynchronize(s);
+    void *ptrs[] = {dV, dW, dH, dHp, d_iters, d_order, d_next, d_insts};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (s) cudaStreamDestroy(s);
+    return st;
+}

@@ -222,6 +222,21 @@ gpunmf_status gpunmf_batch_commit(gpunmf_batch *b);
 /* Overwrite every instance's W and H from host buffers (same shapes as at creation). */
 gpunmf_status gpunmf_batch_reset_factors(gpunmf_batch *b, const float *const *W, const float *const *H);
 
+/* Grouped training, FacesNMFDlg.cpp:582-656 (TrainUsingGroups).  Host, column-major V (n x m),
+ * W (n x r) and H (r x m); W and H are inputs and outputs.  The first blocks = floor(m/group)
+ * blocks of `group` consecutive columns of V are factorised independently with rank
+ * rs = floor(r/blocks), block s starting from W's columns s*rs.. and the diagonal block of H (rows
+ * s*rs.., columns s*group..) -- the reference starts each block from fresh rand() factors.  Each
+ * block iterates its rule until QualityImprovement() changes to a value below tol, the
+ * reference's test, or max_iters.  Results: W's columns s*rs.. and, in the block's columns of H,
+ * the block's H in rows s*rs.. and zeros elsewhere; W columns from blocks*rs and H columns from
+ * blocks*group are returned unchanged.  iterations (nullable) receives `blocks` counts.
+ * The multiplicative Euclidean rule in FP32 with rs <= 32 runs all blocks in one persistent
+ * batched launch; other rules and precisions run one job per block, many at a time. */
+gpunmf_status gpunmf_grouped_train(int rule, int n, int m, int r, int group, const float *V, float *W,
+                                   float *H, float tol, int max_iters, float eps, int precision,
+                                   int *iterations);
+
 /* ------------------------------------------------------------------ */
 /* Serving with continuous batching.  Jobs arrive at any time; a       */
 /* scheduler thread admits each one as soon as one of `slots` stream   */

@@ -153,3 +153,73 @@ def reference_run(rule, V, W, H, iters, updateW=True, residuals=False):
     if rc != 0:
         raise RuntimeError("ref_hostnmf_run failed")
     return (W, H, res) if residuals else (W, H)
+
+
+class QualityLag:
+    """NMF::DetermineQualityImprovement (nmf_base.h:70-89) with every read-back complete: the value
+    read at an iteration is the quality sampled at the previous one (0.0 before the first sample),
+    and the improvement is set from the third sample on.  All values are float32 as in the reference."""
+
+    def __init__(self):
+        self.times = 0
+        self.last = np.float32(-1.0)
+        self.delta = np.float32(1.0)
+        self.value = np.float32(0.0)
+
+    def sample(self, new_value):
+        q = self.value
+        if self.times > 2:
+            self.delta = np.float32(q - self.last)
+        self.times += 1
+        if self.times <= 3:
+            self.times += 1
+        self.last = q
+        self.value = np.float32(new_value)
+
+
+def grouped_run(rule, V, W, H, group, tol, max_iters, eps=1e-8, nthreads=1, iters_per_block=None):
+    """TrainUsingGroups (src/examples/FacesNMF/FacesNMFDlg.cpp:582-656) over the float oracle.
+
+    V's first floor(m/group)*group columns are split into blocks of `group` columns; block s has rank
+    rs = floor(r / blocks) and starts from W[:, s*rs:(s+1)*rs] and the diagonal block
+    H[s*rs:(s+1)*rs, s*group:(s+1)*group] (the reference draws fresh random factors instead).  Each
+    block iterates until its QualityImprovement() changes to a value below tol (the reference's loop,
+    :605-629) or max_iters.  Its W fills the block's columns of W; its H fills the block's rows of
+    the block's columns of H, zeros elsewhere in those columns (:632-651).  Rule 4 is the additive
+    Euclidean rule with the H step skipped.  iters_per_block runs exactly those counts instead of the
+    test.  Returns (W, H, iterations per block, deltas per block).
+    """
+    V = _f32(V)
+    W = _f32(W).copy(order="F")
+    H = _f32(H).copy(order="F")
+    n, m = V.shape
+    r = W.shape[1]
+    blocks = m // group
+    rs = r // blocks
+    iters_out, deltas_out = [], []
+    for s in range(blocks):
+        Vs = np.asfortranarray(V[:, s * group:(s + 1) * group])
+        Ws = np.asfortranarray(W[:, s * rs:(s + 1) * rs])
+        Hs = np.asfortranarray(H[s * rs:(s + 1) * rs, s * group:(s + 1) * group])
+        lag = QualityLag()
+        prev = lag.delta
+        deltas = []
+        k = 0
+        limit = max_iters if iters_per_block is None else iters_per_block[s]
+        while k < limit:
+            lag.sample(quality(Vs, hostnmf_wh(Ws, Hs), eps))
+            Ws, Hs = hostnmf_run(2 if rule == 4 else rule, Vs, Ws, Hs, 1, eps=eps, clamp_sums=True,
+                                 nthreads=nthreads, skip_h=(rule == 4))
+            k += 1
+            q = lag.delta
+            deltas.append(float(q))
+            if q != prev and iters_per_block is None:
+                if q < tol:
+                    break
+                prev = q
+        W[:, s * rs:(s + 1) * rs] = Ws
+        H[:, s * group:(s + 1) * group] = 0.0
+        H[s * rs:(s + 1) * rs, s * group:(s + 1) * group] = Hs
+        iters_out.append(k)
+        deltas_out.append(deltas)
+    return W, H, iters_out, deltas_out

@@ -88,3 +88,20 @@ def test_planted_error_is_caught(golden):
     V[5, 7] = np.nextafter(V[5, 7], np.float32(2.0))
     Wo, Ho = oracle.hostnmf_run(rule, V, W, H, iters, updateW=updateW, eps=1e-8)
     assert not np.array_equal(Wo, data[name + "/W"])
+
+
+def test_oracle_grouped_layout_and_stop():
+    """TrainUsingGroups restated: block layout and the lagged stopping test."""
+    from gpumlib_gb300 import inputs
+    V = inputs.uniform_matrix(21, 30, 47)
+    W, H = inputs.factors(22, 30, 47, 7)
+    Wo, Ho, its, deltas = oracle.grouped_run(1, V, W, H, 15, 0.5, 400)
+    assert len(its) == 3                      # 47 // 15 blocks, rank 7 // 3 = 2 each
+    assert np.array_equal(Wo[:, 6:], W[:, 6:]) and np.array_equal(Ho[:, 45:], H[:, 45:])
+    for s in range(3):
+        block = Ho[:, s * 15:(s + 1) * 15]
+        assert np.all(np.delete(block, np.s_[2 * s:2 * s + 2], axis=0) == 0)
+        d = deltas[s]
+        assert d[0] == 1.0 and d[1] == 1.0    # no improvement before the third sample
+        assert its[s] == len(d) and (d[-1] < 0.5 or its[s] == 400)
+        assert all(x >= 0.5 for x in d[2:-1] if x != 1.0)
