@@ -79,6 +79,12 @@ SIGNATURES = [
     ("gpunmf_grouped_train", ctypes.c_int,
      [ctypes.c_int] * 5 + [ctypes.c_void_p] * 3 + [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int,
                                                     ctypes.c_void_p]),
+    ("gpunmf_faces_scan", ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_void_p] * 3),
+    ("gpunmf_faces_load", ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 5 + [ctypes.c_void_p] * 2),
+    ("gpunmf_faces_load_device", ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 5 + [ctypes.c_void_p] * 3),
+    ("gpunmf_save_csv", ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    ("gpunmf_save_csv_device", ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_void_p]),
     ("gpumlib_cuda_nmf_multiplicative_euclidean_update_matrix", ctypes.c_int,
      [ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("gpumlib_cuda_nmf_multiplicative_divergence_update_matrix_w", ctypes.c_int,
@@ -141,6 +147,10 @@ class GpuNmfError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("gpunmf error %s (%d): %s" % (STATUS.get(status, "?"), status, msg))
         self.status = status
+
+
+def last_error():
+    return load().gpunmf_last_error().decode(errors="replace")
 
 
 def check(status):

@@ -238,6 +238,31 @@ gpunmf_status gpunmf_grouped_train(int rule, int n, int m, int r, int group, con
                                    int *iterations);
 
 /* ------------------------------------------------------------------ */
+/* FacesNMF data set I/O (src/examples/FacesNMF/FacesNMFDlg.cpp).       */
+/* ------------------------------------------------------------------ */
+/* FolderHasImages (:309-347): reads folder/face00001.pgm's P5 header for the image size and counts
+ * the images face00001.pgm.. by the reference's probe (steps of 1024, halved on every miss). */
+gpunmf_status gpunmf_faces_scan(const char *folder, int *count, int *width, int *height);
+
+/* LoadImage (:409-472) for images 1..count into V (width*height x count, column-major FP32), host
+ * (gpunmf_faces_load) or device memory (gpunmf_faces_load_device, on `stream`, NULL = a private one).
+ * equalize: the reference's histogram equalisation; else pixel / 255.  reference_offset = 1 reads the
+ * pixel block where the reference does, starting at the whitespace byte that ends the header (pixel 0
+ * is that byte, the last pixel is not read); 0 reads it where the PGM format puts it.  Images that
+ * fail (format, size, max gray value other than 255, short file) get a zero column, the others are
+ * loaded, and the call returns GPUNMF_ERR_INVALID with *failed (nullable) = how many failed. */
+gpunmf_status gpunmf_faces_load(const char *folder, int count, int width, int height, int equalize,
+                                int reference_offset, float *V, int *failed);
+gpunmf_status gpunmf_faces_load_device(const char *folder, int count, int width, int height, int equalize,
+                                       int reference_offset, float *dV, void *stream, int *failed);
+
+/* Save (:913-924): one line per COLUMN of the rows x cols column-major matrix, its values
+ * comma-separated in fixed notation with 20 decimals (PRECISION, Definitions.h:31), '\n' after each
+ * line.  _device: the matrix is in device memory (read back on `stream`). */
+gpunmf_status gpunmf_save_csv(const char *path, const float *M, int rows, int cols);
+gpunmf_status gpunmf_save_csv_device(const char *path, const float *dM, int rows, int cols, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Serving with continuous batching.  Jobs arrive at any time; a       */
 /* scheduler thread admits each one as soon as one of `slots` stream   */
 /* slots is free and its device footprint fits `hbm_budget_bytes`,     */
