@@ -64,7 +64,28 @@ struct SkParams {
     float *gram_out;
     int gram_count;
     int gram_entries;
+    // fused update (kernel template FNP > 0).  Every CTA owns a contiguous slice of the rows of the
+    // factor X it updates.  While its tensor pipe streams V, two worker warps copy the old rows and
+    // the Gram of the other factor into shared memory and form the denominators X G; after the
+    // GEMM, the whole CTA waits until the tiles its rows belong to have all their partial
+    // products, sums them, writes the new rows, and reduces the Gram of the new factor (two levels,
+    // last arrivals, fixed order) for the next kernel.
+    float *X;                          // FP32 factor updated: H (r x m) or W (n x r), column-major
+    __nv_bfloat16 *Xb;                 // its BF16 copy (Hb row-major / Wb column-major, ld ldb)
+    long long ldb;
+    int is_w, rows_valid, r, additive; // X is W (rows i) or H (rows u); rows_valid rows
+    float eps;
+    const int *slot_ptr, *slot_list;   // each tile's slots in K order
+    int *tile_cnt, *tile_rd;           // per tile: partial products arrived, readers done (reset by the last)
+    const int *tile_readers;           // per tile: how many row chunks read it
+    const float *G_in;                 // npad^2: the complete Gram of the other factor
+    float *G_out;                      // npad^2: the complete Gram of the new factor
+    float *gp, *gg;                    // [grid][npad^2] per-CTA partials, [groups][npad^2] group sums
+    int *grp_cnt, *all_cnt;            // arrivals per group of 8 CTAs; group sums out, finishers done
+    int ngroups;
 };
+
+constexpr int kGramGroup = 8;  // tile Gram partials reduced per group, then the group sums
 
 extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
 
@@ -75,7 +96,441 @@ __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, int *e
     return ok != 0;
 }
 
-__global__ void __launch_bounds__(kGemmThreads, 1)
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// barrier of the four epilogue warps that also ORs a per-thread flag: every thread gets the same
+// answer at the same barrier, so the warps leave a loop together
+__device__ __forceinline__ bool epi_bar_or(bool v) {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((unsigned)v)
+        : "memory");
+    return r != 0;
+}
+
+// Shared memory the fused update needs beside the stage ring (bytes): the Gram for the
+// denominator, a 64-row staging tile, a flag word and the slot lists of two tiles.
+constexpr int kFusedSlots = 15;  // slots per tile the fused update handles (more: the separate update kernel)
+__host__ __device__ constexpr int fused_gram_floats(int np) { return np * np > 64 * np ? np * np : 64 * np; }
+__host__ __device__ constexpr int fused_smem_bytes(int np) {
+    // the Gram area also holds a chunk's denominators (64 x np)
+    return np == 0 ? 0 : fused_gram_floats(np) * 4 + 64 * (np + 4) * 4 + 16 + 2 * (kFusedSlots + 1) * 4 + 64;
+}
+
+// The fused update: while V streams, two worker warps (64 threads, named barrier 2) prepare it
+// beside the four warps that drain TMEM; after the GEMM, all 256 threads of the CTA finish it.
+// Chunks of up to 64 rows are staged as sX[64][NP + 4].  Thread layouts (NT threads):
+//   products:  RPT x APT block of (row, a) per thread
+//   Gram:      NPT entries (row ga of the Gram, columns gb0..) per thread
+template <int NP, int NT>
+struct FusedLayout {
+    static constexpr int LDX = NP + 4;
+    static constexpr int APT = 8, AG = NP / APT, RG = NT / AG, RPT = 64 / RG;
+    static constexpr int TPA = NT / NP, NPT = NP / TPA;
+    static constexpr int SL = 64 * NP / NT;   // staged values per thread
+    static_assert(AG * RG == NT && RG * RPT == 64 && TPA * NP == NT && NPT % 4 == 0, "fused layout");
+};
+
+__device__ __forceinline__ void wk_bar() { asm volatile("bar.sync 2, 64;" ::: "memory"); }
+
+// rows [row0, row0 + nrows) (nrows <= 64) of a factor into sX[rho][a], zero elsewhere, up to 32
+// loads in flight per thread.  w_layout: W(i, a) at a*ld + i (threads along i); else H(a, u) at
+// u*r + a (threads along a).
+template <int NP, int NT>
+__device__ __forceinline__ void stage_rows(const float *__restrict__ X, int w_layout, long long ld, int r,
+                                           long long row0, int nrows, float *sX, int tid) {
+    using L = FusedLayout<NP, NT>;
+    constexpr int B = L::SL < 32 ? L::SL : 32;
+#pragma unroll 1
+    for (int k0 = 0; k0 < L::SL; k0 += B) {
+        float v[B];
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int k = tid + (k0 + q) * NT;
+            if (w_layout) {
+                const int a = k >> 6, rho = k & 63;
+                v[q] = (rho < nrows && a < r) ? X[(long long)a * ld + row0 + rho] : 0.f;
+            } else {
+                const int rho = k / NP, a = k % NP;
+                v[q] = (rho < nrows && a < r) ? X[(row0 + rho) * r + a] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            const int k = tid + (k0 + q) * NT;
+            if (w_layout) sX[(k & 63) * L::LDX + (k >> 6)] = v[q];
+            else sX[(k / NP) * L::LDX + k % NP] = v[q];
+        }
+    }
+}
+
+// The same staging as asynchronous copies (cp.async, zero-filled outside the rows / r), issued and
+// committed but not waited for: all of them are in flight at once, which matters while V streams.
+// vec16: H rows copied 16 bytes at a time (r a multiple of 4, so every row starts 16-byte aligned).
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(float *dst, const float *src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int NP, int NT>
+__device__ __forceinline__ void stage_rows_async(const float *__restrict__ X, int w_layout, long long ld, int r,
+                                                 long long row0, int nrows, float *sX, int tid, bool vec16) {
+    using L = FusedLayout<NP, NT>;
+    if (!w_layout && vec16) {
+        for (int k = tid; k < 64 * NP / 4; k += NT) {
+            const int rho = k / (NP / 4), a = (k % (NP / 4)) * 4;
+            const bool ok = rho < nrows && a < r;
+            cp_async16(sX + rho * L::LDX + a, ok ? X + (row0 + rho) * r + a : X, ok);
+        }
+    } else {
+        for (int k = tid; k < 64 * NP; k += NT) {
+            int rho, a;
+            const float *src;
+            if (w_layout) {
+                a = k >> 6; rho = k & 63;
+                src = X + (long long)a * ld + row0 + rho;
+            } else {
+                rho = k / NP; a = k % NP;
+                src = X + (row0 + rho) * r + a;
+            }
+            const bool ok = rho < nrows && a < r;
+            cp_async4(sX + rho * L::LDX + a, ok ? src : X, ok);
+        }
+    }
+    cp_async_commit();
+}
+
+// den = X G for the staged chunk (b in order, fmaf(G[b][a], x[b], den) as the separate update
+// kernel forms them), then stored over the Gram area as sD[rho][a] after `bar` (every thread is
+// done reading G)
+template <int NP, int NT, class Bar>
+__device__ __forceinline__ void chunk_denominators(const float *sX, float *sG, int tid, Bar bar) {
+    using L = FusedLayout<NP, NT>;
+    const int a0 = (tid % L::AG) * L::APT, r0 = (tid / L::AG) * L::RPT;
+    float den[L::RPT][L::APT];
+#pragma unroll
+    for (int k = 0; k < L::RPT; k++)
+#pragma unroll
+        for (int q = 0; q < L::APT; q++) den[k][q] = 0.f;
+#pragma unroll 1
+    for (int b = 0; b < NP; b += 4) {
+        float4 xr[L::RPT];
+#pragma unroll
+        for (int k = 0; k < L::RPT; k++) xr[k] = *reinterpret_cast<const float4 *>(sX + (r0 + k) * L::LDX + b);
+#pragma unroll
+        for (int jb = 0; jb < 4; jb++) {
+            float gv[L::APT];
+#pragma unroll
+            for (int cc = 0; cc < L::APT / 4; cc++) {
+                const float4 g4 = *reinterpret_cast<const float4 *>(sG + (b + jb) * NP + a0 + 4 * cc);
+                gv[4 * cc] = g4.x; gv[4 * cc + 1] = g4.y; gv[4 * cc + 2] = g4.z; gv[4 * cc + 3] = g4.w;
+            }
+#pragma unroll
+            for (int k = 0; k < L::RPT; k++) {
+                const float xv = jb == 0 ? xr[k].x : jb == 1 ? xr[k].y : jb == 2 ? xr[k].z : xr[k].w;
+#pragma unroll
+                for (int q = 0; q < L::APT; q++) den[k][q] = fmaf(gv[q], xv, den[k][q]);
+            }
+        }
+    }
+    bar();
+#pragma unroll
+    for (int k = 0; k < L::RPT; k++)
+#pragma unroll
+        for (int cc = 0; cc < L::APT / 4; cc++)
+            *reinterpret_cast<float4 *>(sG + (r0 + k) * NP + a0 + 4 * cc) =
+                make_float4(den[k][4 * cc], den[k][4 * cc + 1], den[k][4 * cc + 2], den[k][4 * cc + 3]);
+}
+
+// Prologue of the fused update (the two worker warps, while V streams): the old rows of this
+// CTA's first chunk and the complete Gram of the other factor copied into shared memory (all
+// copies in flight at once), then the chunk's denominators (left in sG as sD).
+template <int NP>
+__device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float *sG, float *sX) {
+    constexpr int E = NP * NP;
+    const int c = blockIdx.x, G = gridDim.x;
+    const long long x0 = (long long)c * pr.rows_valid / G, x1 = (long long)(c + 1) * pr.rows_valid / G;
+    stage_rows_async<NP, 64>(pr.X, pr.is_w, pr.rows_valid, pr.r, x0, (int)min(64LL, x1 - x0), sX, wt,
+                             (pr.r & 3) == 0);
+    for (int k = wt; k < E / 4; k += 64) cp_async16(sG + 4 * k, pr.G_in + 4 * k, true);
+    cp_async_commit();
+    cp_async_wait_all();
+    wk_bar();
+    chunk_denominators<NP, 64>(sX, sG, wt, wk_bar);
+}
+
+// Tail of the fused update (all 256 threads, after the GEMM): per chunk of this CTA's rows, wait
+// until the chunk's tiles have all their partial products, sum them in K order,
+// X_new = X num / (den + eps) or max(0, X + X / den (num - den)), write X and its BF16 copy and
+// add the new rows to this CTA's Gram partial; then the two-level reduction of the partials into
+// the complete Gram of the new factor (the last CTA of a group of 8 sums the group, the last group
+// sums the groups, each in a fixed order, so the result does not depend on arrival order).
+template <int NP>
+__device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *sG, float *sX, int *sflag, int *sSl) {
+    constexpr int NT = 256;
+    using L = FusedLayout<NP, NT>;
+    constexpr int E = NP * NP;
+    constexpr int GB = NP / 16;  // Gram partial: a GB x GB block per thread (16 x 16 threads)
+    constexpr int kMaxBatch = 4; // slots whose loads are issued together
+    const int c = blockIdx.x, G = gridDim.x;
+    float *const X = pr.X;
+    __nv_bfloat16 *const Xb = pr.Xb;
+    const float *const partials = pr.partials;
+    int *const err = pr.err;
+    const long long ldb = pr.ldb;
+    const int is_w = pr.is_w, r = pr.r, rows = pr.rows_valid, additive = pr.additive;
+    const float eps = pr.eps;
+    const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
+    const int a0 = (tid % L::AG) * L::APT, r0 = (tid / L::AG) * L::RPT;
+    const int ga0 = (tid >> 4) * GB, gb0 = (tid & 15) * GB;
+    float *const gpc = pr.gp + (size_t)c * E;
+    const float *sD = sG;
+    auto bar = [] { __syncthreads(); };
+    float gacc[GB][GB];
+#pragma unroll
+    for (int i = 0; i < GB; i++)
+#pragma unroll
+        for (int k = 0; k < GB; k++) gacc[i][k] = 0.f;
+#pragma unroll 1
+    for (long long xb = x0; xb < x1; xb += 64) {
+        const int nr = (int)min(64LL, x1 - xb);
+        if (xb != x0) {  // later chunks (more than 64 rows per CTA): stage, reload G, denominators
+            __syncthreads();
+            stage_rows<NP, NT>(X, is_w, rows, r, xb, nr, sX, tid);
+            for (int k = tid; k < E / 4; k += NT)
+                reinterpret_cast<float4 *>(sG)[k] = __ldcg(reinterpret_cast<const float4 *>(pr.G_in) + k);
+            __syncthreads();
+            chunk_denominators<NP, NT>(sX, sG, tid, bar);
+        }
+        const int t0 = (int)(xb / kTileM), t1 = (int)((xb + nr - 1) / kTileM);  // t1 <= t0 + 1
+        if (tid == 0) {
+            bool ok = true;
+            for (int t = t0; t <= t1 && ok; t++)
+                ok = flag_wait_ge(pr.tile_cnt + t, pr.slot_ptr[t + 1] - pr.slot_ptr[t], err, kErrWaitTile);
+            *sflag = ok ? 1 : 0;
+        }
+        // the chunk's slot lists (at most kFusedSlots per tile, checked on the host)
+        if (tid < 2 && t0 + tid <= t1) {
+            const int t = t0 + tid, q0 = pr.slot_ptr[t], ns = pr.slot_ptr[t + 1] - q0;
+            sSl[tid * (kFusedSlots + 1)] = ns;
+            for (int q = 0; q < ns; q++) sSl[tid * (kFusedSlots + 1) + 1 + q] = pr.slot_list[q0 + q];
+        }
+        __syncthreads();
+        if (!*sflag) return;  // uniform
+        __threadfence();
+        float num[L::RPT][L::APT];
+#pragma unroll
+        for (int k = 0; k < L::RPT; k++)
+#pragma unroll
+            for (int q = 0; q < L::APT; q++) num[k][q] = 0.f;
+        {
+            int tk[L::RPT], lr[L::RPT];
+#pragma unroll
+            for (int k = 0; k < L::RPT; k++) {
+                const long long grow = xb + r0 + k;
+                tk[k] = (int)(grow / kTileM) - t0;
+                lr[k] = (int)(grow % kTileM);
+            }
+            const int nsmax = max(sSl[0], t1 > t0 ? sSl[kFusedSlots + 1] : 0);
+            for (int q0 = 0; q0 < nsmax; q0 += kMaxBatch) {  // the loads of up to kMaxBatch slots together
+                float4 v[kMaxBatch][L::RPT][2];
+#pragma unroll
+                for (int qq = 0; qq < kMaxBatch; qq++)
+#pragma unroll
+                    for (int k = 0; k < L::RPT; k++) {
+                        const int *sl = sSl + tk[k] * (kFusedSlots + 1);
+                        const int q = q0 + qq;
+                        if (r0 + k < nr && q < sl[0]) {
+                            const float4 *src = reinterpret_cast<const float4 *>(
+                                partials + ((size_t)sl[1 + q] * kTileM + lr[k]) * NP + a0);
+                            v[qq][k][0] = __ldcg(src);
+                            v[qq][k][1] = __ldcg(src + 1);
+                        } else {
+                            v[qq][k][0] = v[qq][k][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
+                    }
+#pragma unroll
+                for (int qq = 0; qq < kMaxBatch; qq++)  // slots in K order
+#pragma unroll
+                    for (int k = 0; k < L::RPT; k++) {
+                        num[k][0] += v[qq][k][0].x; num[k][1] += v[qq][k][0].y;
+                        num[k][2] += v[qq][k][0].z; num[k][3] += v[qq][k][0].w;
+                        num[k][4] += v[qq][k][1].x; num[k][5] += v[qq][k][1].y;
+                        num[k][6] += v[qq][k][1].z; num[k][7] += v[qq][k][1].w;
+                    }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < L::RPT; k++)
+#pragma unroll
+            for (int q = 0; q < L::APT; q++) {
+                const int a = a0 + q;
+                const float xv = sX[(r0 + k) * L::LDX + a], d = sD[(r0 + k) * NP + a], nv = num[k][q];
+                float v = 0.f;
+                if (r0 + k < nr && a < r) {
+                    if (additive) {
+                        v = xv + (xv / d) * (nv - d);
+                        v = v < 0.f ? 0.f : v;
+                    } else {
+                        v = xv * (nv / (d + eps));
+                    }
+                }
+                num[k][q] = v;
+            }
+        __syncthreads();  // old rows and partial slots read by every thread
+        if (tid == 0)
+            for (int t = t0; t <= t1; t++)
+                if (atomicAdd(pr.tile_rd + t, 1) == pr.tile_readers[t] - 1) {  // the last reader resets
+                    pr.tile_cnt[t] = 0;
+                    pr.tile_rd[t] = 0;
+                }
+#pragma unroll
+        for (int k = 0; k < L::RPT; k++)
+#pragma unroll
+            for (int cc = 0; cc < L::APT / 4; cc++)
+                *reinterpret_cast<float4 *>(sX + (r0 + k) * L::LDX + a0 + 4 * cc) =
+                    make_float4(num[k][4 * cc], num[k][4 * cc + 1], num[k][4 * cc + 2], num[k][4 * cc + 3]);
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < L::SL; kk++) {
+            const int k = tid + kk * NT;
+            if (is_w) {
+                const int a = k >> 6, rho = k & 63;
+                if (rho < nr && a < r) {
+                    const float v = sX[rho * L::LDX + a];
+                    X[(long long)a * rows + xb + rho] = v;
+                    Xb[(long long)a * ldb + xb + rho] = __float2bfloat16_rn(v);
+                }
+            } else {
+                const int rho = k / NP, a = k % NP;
+                if (rho < nr && a < r) X[(xb + rho) * r + a] = sX[rho * L::LDX + a];
+                const int a2 = k >> 6, rho2 = k & 63;
+                if (rho2 < nr && a2 < r) Xb[(long long)a2 * ldb + xb + rho2] = __float2bfloat16_rn(sX[rho2 * L::LDX + a2]);
+            }
+        }
+        // this chunk's new rows into this CTA's Gram partial, rows in order
+#pragma unroll 2
+        for (int rr = 0; rr < nr; rr++) {
+            float xa[GB], xb2[GB];
+#pragma unroll
+            for (int i = 0; i < GB; i++) {
+                xa[i] = sX[rr * L::LDX + ga0 + i];
+                xb2[i] = sX[rr * L::LDX + gb0 + i];
+            }
+#pragma unroll
+            for (int i = 0; i < GB; i++)
+#pragma unroll
+                for (int k = 0; k < GB; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < GB; i++)
+#pragma unroll
+        for (int k = 0; k < GB; k++) gpc[(ga0 + i) * NP + gb0 + k] = gacc[i][k];
+    // two-level reduction of the CTAs' partials into G_out
+    __threadfence();
+    __syncthreads();
+    const int g = c / kGramGroup, gsize = min(kGramGroup, G - g * kGramGroup);
+    if (tid == 0) *sflag = atomicAdd(pr.grp_cnt + g, 1) == gsize - 1 ? 1 : 0;
+    __syncthreads();
+    if (*sflag) {
+        __threadfence();
+        constexpr int EPT = E / NT;
+        const float *src = pr.gp + (size_t)g * kGramGroup * E;
+        float sum[EPT];
+#pragma unroll
+        for (int k = 0; k < EPT; k++) sum[k] = 0.f;
+        {
+            float v[kGramGroup][EPT];
+#pragma unroll
+            for (int q = 0; q < kGramGroup; q++)
+#pragma unroll
+                for (int k = 0; k < EPT; k++) v[q][k] = q < gsize ? __ldcg(src + (size_t)q * E + tid + k * NT) : 0.f;
+#pragma unroll
+            for (int q = 0; q < kGramGroup; q++)
+#pragma unroll
+                for (int k = 0; k < EPT; k++)
+                    if (q < gsize) sum[k] += v[q][k];
+        }
+#pragma unroll
+        for (int k = 0; k < EPT; k++) pr.gg[(size_t)g * E + tid + k * NT] = sum[k];
+        __threadfence();
+        __syncthreads();
+        // second level, spread over the group finishers: each waits until every group sum is out,
+        // then sums its slice of the entries over the groups in order
+        const int ng = pr.ngroups;
+        if (tid == 0) {
+            pr.grp_cnt[g] = 0;
+            atomicAdd(pr.all_cnt, 1);
+            *sflag = flag_wait_ge(pr.all_cnt, ng, err, kErrWaitGram) ? 1 : 0;
+        }
+        __syncthreads();
+        if (*sflag) {
+            __threadfence();
+            const int e0 = (int)((long long)g * E / ng), e1 = (int)((long long)(g + 1) * E / ng);
+            for (int e = e0 + tid; e < e1; e += NT) {
+                float v[32];
+                float acc = 0.f;
+                for (int q0 = 0; q0 < ng; q0 += 32) {
+#pragma unroll
+                    for (int q = 0; q < 32; q++) v[q] = q0 + q < ng ? __ldcg(pr.gg + (size_t)(q0 + q) * E + e) : 0.f;
+#pragma unroll
+                    for (int q = 0; q < 32; q++)
+                        if (q0 + q < ng) acc += v[q];
+                }
+                pr.G_out[e] = acc;
+            }
+            __syncthreads();
+            if (tid == 0 && atomicAdd(pr.all_cnt + 1, 1) == ng - 1) {  // the last finisher resets
+                pr.all_cnt[1] = 0;
+                atomicExch(pr.all_cnt, 0);
+            }
+        }
+    }
+}
+
+// Gram partials of a factor for the first fused kernel: CTA c over rows [c*rows/G, (c+1)*rows/G),
+// the row partition the fused kernels use, so the partials match the ones they leave.
+template <int NP>
+__global__ void __launch_bounds__(64) gram_partials_kernel(const float *__restrict__ X, int w_layout, int rows,
+                                                            int r, float *__restrict__ out) {
+    using L = FusedLayout<NP, 64>;
+    __shared__ __align__(16) float sX[64 * L::LDX];
+    const int wt = threadIdx.x, c = blockIdx.x, G = gridDim.x;
+    const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
+    const int ga = wt / L::TPA, gb0 = (wt % L::TPA) * L::NPT;
+    float gacc[L::NPT];
+#pragma unroll
+    for (int k = 0; k < L::NPT; k++) gacc[k] = 0.f;
+    for (long long xb = x0; xb < x1; xb += 64) {
+        const int nr = (int)min(64LL, x1 - xb);
+        __syncthreads();
+        stage_rows<NP, 64>(X, w_layout, rows, r, xb, nr, sX, wt);
+        __syncthreads();
+        for (int rr = 0; rr < nr; rr++) {
+            const float xa = sX[rr * L::LDX + ga];
+#pragma unroll
+            for (int k = 0; k < L::NPT; k++) gacc[k] = fmaf(xa, sX[rr * L::LDX + gb0 + k], gacc[k]);
+        }
+    }
+    for (int k = 0; k < L::NPT; k++) out[(size_t)c * NP * NP + ga * NP + gb0 + k] = gacc[k];
+}
+
+// threads of the GEMM: producer, MMA issuer, four TMEM-draining warps, and with a fused update
+// two worker warps
+__host__ __device__ constexpr int gemm_threads(int fnp) { return fnp ? kGemmThreads + 64 : kGemmThreads; }
+
+template <int FNP>
+__global__ void __launch_bounds__(gemm_threads(FNP), 1)
     tc_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       SkParams p) {
     const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
@@ -89,6 +544,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     uint64_t *tempty = tfull + 2;        // [2]
     uint64_t *mdone = tempty + 2;        // [1]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+    // fused-update areas (FNP > 0): Gram, 64-row staging tile, flag
+    float *sG = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tmem_slot + 4) + 15) & ~uintptr_t(15));
+    float *sX = sG + fused_gram_floats(FNP);
+    int *sflag = reinterpret_cast<int *>(sX + 64 * (FNP + 4));
+    int *sSl = sflag + 4;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long T = (long long)p.tiles * p.kblocks;
@@ -197,11 +657,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             tc_commit(mdone);
             mbar_wait_quiet(mdone, 0);
         }
-    } else {
+    } else if (warp < 6) {
         // While the first accumulator fills, finish the Gram matrix the update kernel of the
         // previous half-step left as per-CTA partials: this CTA owns entries
         // [c*E/G, (c+1)*E/G); four lanes share an entry and sum the partials in a fixed order.
-        if (p.gram_out) {
+        if (FNP == 0 && p.gram_out) {
             const int et = threadIdx.x - 64;  // 0..127
             const long long E = p.gram_entries;
             const long long e0 = (long long)blockIdx.x * E / gridDim.x, e1 = (long long)(blockIdx.x + 1) * E / gridDim.x;
@@ -231,7 +691,12 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         for (long long b = lo; b < hi;) {
             const long long t = b / p.kblocks;
             const long long e = min(hi, (t + 1) * p.kblocks);
-            if (!warp_wait(&tfull[acc], aphase, p.err, kErrWaitTmemFull)) break;
+            const bool ok = warp_wait(&tfull[acc], aphase, p.err, kErrWaitTmemFull);
+            if constexpr (FNP > 0) {
+                if (epi_bar_or(!ok)) break;  // the fused epilogue's barriers need all four warps
+            } else if (!ok) {
+                break;
+            }
             tc_fence_after();
             float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
             const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * p.npad);
@@ -252,11 +717,25 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 acc = 0;
                 aphase ^= 1;
             }
+            if constexpr (FNP > 0) {
+                // this segment's partial product is out: count it on its tile
+                __threadfence();
+                epi_bar();
+                if (threadIdx.x == 64) atomicAdd(&p.tile_cnt[t], 1);
+            }
             seg++;
             b = e;
         }
+    } else if constexpr (FNP > 0) {
+        fused_prologue<FNP>(p, threadIdx.x - kGemmThreads, sG, sX);  // warps 6 and 7
     }
     __syncthreads();
+    if constexpr (FNP > 0) {
+        // every role is done: all threads finish the update (skipped, uniformly, after an error)
+        const bool go = __syncthreads_and(*((volatile int *)p.err) == 0);
+        if (go) fused_tail<FNP>(p, threadIdx.x, sG, sX, sflag, sSl);
+        __syncthreads();
+    }
     if (warp == 0) {
         tc_fence_after();
         tmem_dealloc(tmem, p.tmem_cols);
@@ -999,8 +1478,11 @@ struct TcGemm {
     gpunmf::SkParams p;
     int grid = 0;
     int smem = 0;
+    int fnp = 0;  // fused update rank (kernel template argument), 0 = separate update kernel
     int *slot_ptr = nullptr, *slot_list = nullptr;
     int *tile_slots = nullptr;
+    int *counters = nullptr;  // [tiles] tile arrivals, [groups] group arrivals, [1] total
+    float *grams = nullptr;   // [tiles + groups][npad^2] tile Gram partials and group sums
 };
 
 struct KlGemm {
@@ -1105,11 +1587,26 @@ static void schedule(int tiles, int kblocks, int G, int *max_seg, std::vector<in
     *max_seg = ms;
 }
 
-static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int npad, float **partials, int *err) {
+static int smem_optin() {
+    static int v = 0;
+    if (!v) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
+            v = 227 * 1024;
+    }
+    return v;
+}
+
+static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int npad, float **partials, int *err,
+                                int fnp = 0) {
     const int tiles = ceil_div(rows, kTileM);
     const int boxB = npad * kBlockK * 2;
+    // the fused epilogue's areas take shared memory from the stage ring; the separate update kernel
+    // needs room beside a GEMM CTA instead
+    const int budget = fnp ? smem_optin() - fused_smem_bytes(fnp) - 64 : kSmemBudget;
     // two 64-wide boxes per stage when at least three such stages fit, else one
-    const int bps = (kSmemBudget - 1280) / (2 * (kStageABytes + boxB)) >= 3 ? 2 : 1;
+    const int bps = (budget - 1280) / (2 * (kStageABytes + boxB)) >= 3 ? 2 : 1;
     const int kblocks = ceil_div(K, kBlockK * bps);
     const long long T = (long long)tiles * kblocks;
     g.grid = (int)std::min<long long>(num_sms(), T);
@@ -1126,7 +1623,7 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
             for (int q = ptr[t]; q < ptr[t + 1]; q++) table[(size_t)t * kSlotW + (q - ptr[t])] = list[q];
     }
     const int stage_bytes = bps * (kStageABytes + boxB);
-    int stages = std::min(kMaxStages, (kSmemBudget - 1024 - 256) / stage_bytes);
+    int stages = std::min(kMaxStages, (budget - 1024 - 256) / stage_bytes);
     g.p.bps = bps;
     g.p.tiles = tiles;
     g.p.kblocks = kblocks;
@@ -1137,7 +1634,8 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     while (cols < (uint32_t)(2 * npad)) cols <<= 1;
     g.p.tmem_cols = cols;
     g.p.err = err;
-    g.smem = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16;
+    g.smem = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16 + (fnp ? 16 + fused_smem_bytes(fnp) : 0);
+    g.fnp = fnp;
     size_t slots = (size_t)g.grid * max_seg;
     cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_ptr, ptr.size() * sizeof(int));
@@ -1154,7 +1652,69 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
         return GPUNMF_ERR_NOMEM;
     }
     g.p.partials = *partials;
+    g.p.slot_ptr = g.slot_ptr;
+    g.p.slot_list = g.slot_list;
+    if (fnp) {
+        // per tile: arrivals, readers done, readers expected; the Gram slice counters; per CTA the
+        // Gram partial of its new rows
+        const int G = g.grid;
+        std::vector<int> readers(tiles, 0);
+        for (int c = 0; c < G; c++) {
+            const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
+            for (long long xb = x0; xb < x1; xb += 64) {
+                const long long xe = std::min(x1, xb + 64);
+                for (long long t = xb / kTileM; t <= (xe - 1) / kTileM; t++) readers[t]++;
+            }
+        }
+        const int groups = ceil_div(G, kGramGroup);
+        const size_t nc = (size_t)3 * tiles + groups + 2;
+        e = job_dev_alloc(j, (void **)&g.counters, nc * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(g.counters, 0, nc * sizeof(int), j->stream);
+        if (e == cudaSuccess) e = job_h2d(j, g.counters + 2 * tiles, readers.data(), tiles * sizeof(int));
+        if (e == cudaSuccess)
+            e = job_dev_alloc(j, (void **)&g.grams, (size_t)(G + groups) * fnp * fnp * sizeof(float));
+        if (e != cudaSuccess) {
+            set_error("fused-update workspace allocation failed: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            return GPUNMF_ERR_NOMEM;
+        }
+        g.p.tile_cnt = g.counters;
+        g.p.tile_rd = g.counters + tiles;
+        g.p.tile_readers = g.counters + 2 * tiles;
+        g.p.grp_cnt = g.counters + 3 * tiles;
+        g.p.all_cnt = g.p.grp_cnt + groups;
+        g.p.gp = g.grams;
+        g.p.gg = g.grams + (size_t)G * fnp * fnp;
+        g.p.ngroups = groups;
+    }
     return GPUNMF_OK;
+}
+
+// Largest number of stream-K segments on one tile for this GEMM shape (the fused update reads at
+// most kFusedSlots per tile); mirrors setup_gemm's schedule.
+static int schedule_max_slots(int rows, int K, int npad, int fnp) {
+    const int tiles = ceil_div(rows, kTileM);
+    const int boxB = npad * kBlockK * 2;
+    const int budget = fnp ? smem_optin() - fused_smem_bytes(fnp) - 64 : kSmemBudget;
+    const int bps = (budget - 1280) / (2 * (kStageABytes + boxB)) >= 3 ? 2 : 1;
+    const int kblocks = ceil_div(K, kBlockK * bps);
+    const int grid = (int)std::min<long long>(num_sms(), (long long)tiles * kblocks);
+    std::vector<int> ptr, list;
+    int max_seg = 1;
+    schedule(tiles, kblocks, grid, &max_seg, ptr, list);
+    int mx = 0;
+    for (int t = 0; t < tiles; t++) mx = std::max(mx, ptr[t + 1] - ptr[t]);
+    return mx;
+}
+
+// rank of the fused update for a Euclidean job (npad 32 or 64), else 0
+static int fused_rank(int npad) { return (npad == 32 || npad == 64) ? npad : 0; }
+
+static size_t fused_bytes(int rows, int npad) {
+    const int np = fused_rank(npad);
+    if (!np) return 0;
+    const int tiles = ceil_div(rows, kTileM), groups = ceil_div(kNumSMsGB300, kGramGroup);
+    return (size_t)(3 * tiles + groups + 2) * sizeof(int) + (size_t)(kNumSMsGB300 + groups) * np * np * sizeof(float);
 }
 
 static size_t gemm_partial_bytes(int rows, int K, int npad) {
@@ -1174,7 +1734,11 @@ static cudaError_t set_gemm_smem_once() {
         cudaGetDevice(&dev);
         result = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (result == cudaSuccess)
-            result = cudaFuncSetAttribute(tc_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+            result = cudaFuncSetAttribute(tc_gemm_sk_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (result == cudaSuccess)
+            result = cudaFuncSetAttribute(tc_gemm_sk_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (result == cudaSuccess)
+            result = cudaFuncSetAttribute(tc_gemm_sk_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
     return result;
 }
@@ -1455,6 +2019,7 @@ size_t tc_footprint(int rule, int n, int m, int r) {
     size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r);
     b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
     b += (size_t)npad * npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
+    b += fused_bytes(m, npad) + fused_bytes(n, npad);
     return b;
 }
 
@@ -1487,18 +2052,36 @@ gpunmf_status tc_create(gpunmf_job *j) {
         cudaGetLastError();
         return GPUNMF_ERR_NOMEM;
     }
-    gpunmf_status st = setup_gemm(j, t->gh, m, n, t->npad, &t->P_h, t->err);
-    if (st == GPUNMF_OK) st = setup_gemm(j, t->gw, n, m, t->npad, &t->P_w, t->err);
+    int fnp = fused_rank(t->npad);
+    if (fnp && (schedule_max_slots(m, n, t->npad, fnp) > kFusedSlots || schedule_max_slots(n, m, t->npad, fnp) > kFusedSlots))
+        fnp = 0;
+    gpunmf_status st = setup_gemm(j, t->gh, m, n, t->npad, &t->P_h, t->err, fnp);
+    if (st == GPUNMF_OK) st = setup_gemm(j, t->gw, n, m, t->npad, &t->P_w, t->err, fnp);
     if (st != GPUNMF_OK) return st;
-    // the H-step GEMM finishes W'W from the W-step update's partials, and vice versa
-    t->gh.p.gram_partials = t->GP_w;
-    t->gh.p.gram_out = t->G_w;
-    t->gh.p.gram_count = t->gp_w_count;
-    t->gh.p.gram_entries = (int)rp2;
-    t->gw.p.gram_partials = t->GP_h;
-    t->gw.p.gram_out = t->G_h;
-    t->gw.p.gram_count = t->gp_h_count;
-    t->gw.p.gram_entries = (int)rp2;
+    if (fnp) {
+        // each GEMM updates its factor itself and leaves that factor's complete Gram for the other
+        // each GEMM takes the Gram the other left (W'W for the H-step, H H' for the W-step) and
+        // leaves the Gram of the factor it updates
+        auto fill = [&](SkParams &q, float *X, __nv_bfloat16 *Xb, long long ldb, int is_w, int rows,
+                        const float *G_in, float *G_out) {
+            q.X = X; q.Xb = Xb; q.ldb = ldb; q.is_w = is_w; q.rows_valid = rows; q.r = r;
+            q.additive = rule_is_additive(j->rule) ? 1 : 0; q.eps = j->eps;
+            q.G_in = G_in; q.G_out = G_out;
+            q.gram_out = nullptr;
+        };
+        fill(t->gh.p, j->H, t->Hb, t->ldh, 0, m, t->G_w, t->G_h);   // H-step: den = W'W H
+        fill(t->gw.p, j->W, t->Wb, t->ldw, 1, n, t->G_h, t->G_w);   // W-step: den = W H H'
+    } else {
+        // the H-step GEMM finishes W'W from the W-step update's partials, and vice versa
+        t->gh.p.gram_partials = t->GP_w;
+        t->gh.p.gram_out = t->G_w;
+        t->gh.p.gram_count = t->gp_w_count;
+        t->gh.p.gram_entries = (int)rp2;
+        t->gw.p.gram_partials = t->GP_h;
+        t->gw.p.gram_out = t->G_h;
+        t->gw.p.gram_count = t->gp_h_count;
+        t->gw.p.gram_entries = (int)rp2;
+    }
     // H-step: rows = u (columns of V): A = Vb (dim0 i over n, dim1 u over m); B = Wb (dim0 i, dim1 a)
     st = make_map(&t->gh.tmA, t->Vb, n, m, t->ldv, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->gh.tmB, t->Wb, n, r, t->ldw, t->npad);
@@ -1537,6 +2120,28 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
         GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 0), t->npad, true, s));
         return GPUNMF_OK;
     }
+    if (t->gh.fnp) {
+        // the complete Gram of the initial W for the first H-step (and of the fixed H for a rule
+        // without an H step): per-CTA partials, then their sum
+        const long long E = (long long)t->npad * t->npad;
+        const int G = t->gw.grid;
+        switch (t->gh.fnp) {
+#define GP(NP)                                                                                          \
+    case NP:                                                                                            \
+        gram_partials_kernel<NP><<<G, 64, 0, s>>>(j->W, 1, j->n, j->r, t->gw.grams);                   \
+        GPUNMF_CUDA_TRY(cudaGetLastError());                                                            \
+        GPUNMF_CUDA_TRY(sum_partials(t->G_w, t->gw.grams, G, E, s));                                   \
+        if (j->rule == GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H) {                                             \
+            gram_partials_kernel<NP><<<G, 64, 0, s>>>(j->H, 0, j->m, j->r, t->gw.grams);               \
+            GPUNMF_CUDA_TRY(cudaGetLastError());                                                        \
+            GPUNMF_CUDA_TRY(sum_partials(t->G_h, t->gw.grams, G, E, s));                               \
+        }                                                                                               \
+        break;
+            GP(32) GP(64)
+#undef GP
+        }
+        return GPUNMF_OK;
+    }
     // Gram partials of the initial W, finished by the first H-step GEMM
     GPUNMF_CUDA_TRY(launch_update(update_params_w(j, 0), t->npad, true, s));
     // a rule without an H step: the Gram partials of the (fixed) H, finished by every W-step GEMM
@@ -1548,7 +2153,7 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
 static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.grid);
-    cfg.blockDim = dim3(kGemmThreads);
+    cfg.blockDim = dim3(gemm_threads(g.fnp));
     cfg.dynamicSmemBytes = g.smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
@@ -1556,7 +2161,11 @@ static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel, g.tmA, g.tmB, g.p);
+    switch (g.fnp) {
+        case 32: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<32>, g.tmA, g.tmB, g.p);
+        case 64: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<64>, g.tmA, g.tmB, g.p);
+        default: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<0>, g.tmA, g.tmB, g.p);
+    }
 }
 
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
@@ -1581,6 +2190,21 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
         mark_end(j);
         GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 1), t->npad, true, s));
         j->launches += 2;
+        return GPUNMF_OK;
+    }
+    if (t->gh.fnp) {
+        // one launch per half-step: the GEMM's last arrivals update the factor and its Gram
+        if (j->rule != GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H) {
+            mark_begin(j);
+            GPUNMF_CUDA_TRY(launch_gemm(t->gh, s));
+            mark_end(j);
+            j->launches += 1;
+        }
+        if (!updateW) return GPUNMF_OK;
+        mark_begin(j);
+        GPUNMF_CUDA_TRY(launch_gemm(t->gw, s));
+        mark_end(j);
+        j->launches += 1;
         return GPUNMF_OK;
     }
     // H <- H .* (W'V) ./ (W'W H + eps), or the additive step; the GEMM also finishes W'W
@@ -1619,7 +2243,7 @@ void tc_destroy(gpunmf_job *j) {
                     t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list,
                     t->gh.tile_slots, t->gw.tile_slots, t->Wr, t->Hc, t->S_w, t->S_h, t->SP_w, t->SP_h,
                     t->kh.slot_ptr, t->kh.slot_list, t->kh.tile_slots, t->kw.slot_ptr, t->kw.slot_list,
-                    t->kw.tile_slots};
+                    t->kw.tile_slots, t->gh.counters, t->gh.grams, t->gw.counters, t->gw.grams};
     for (void *p : ptrs) job_dev_free(j, p);
     delete t;
     j->tc = nullptr;

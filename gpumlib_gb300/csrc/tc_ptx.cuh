@@ -22,6 +22,8 @@ enum ErrorBits : int {
     kErrWaitEmpty = 2,
     kErrWaitTmemFull = 4,
     kErrWaitTmemEmpty = 8,
+    kErrWaitTile = 16,   // a tile's partial products never all arrived
+    kErrWaitGram = 32,   // the grid's Gram reduction never completed
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -82,6 +84,23 @@ __device__ __forceinline__ bool mbar_wait_quiet(uint64_t *bar, uint32_t parity) 
     while (!mbar_try_wait(bar, parity))
         if (clock64() - t0 > kWaitLimitCycles) return false;
     return true;
+}
+
+// Bounded wait until the global word at addr (raised by other CTAs of the same grid) is >= target.
+// Returns false (and sets err_bit in *err) on timeout or if another thread already failed.
+__device__ __forceinline__ bool flag_wait_ge(const int *addr, int target, int *err, int err_bit) {
+    const long long t0 = clock64();
+    for (;;) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(addr) : "memory");
+        if (v >= target) return true;
+        if (*((volatile int *)err) != 0) return false;
+        if (clock64() - t0 > kWaitLimitCycles) {
+            atomicOr(err, err_bit);
+            return false;
+        }
+        __nanosleep(64);
+    }
 }
 
 // ---------------------------------------------------------------- programmatic dependent launch
