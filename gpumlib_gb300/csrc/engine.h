@@ -84,6 +84,9 @@ size_t tc_footprint(int rule, int n, int m, int r);
 gpunmf_status tc_create(gpunmf_job *j);
 gpunmf_status tc_prepare(gpunmf_job *j);  // after V/W/H are uploaded
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW);
+// quality of the current factors on the tensor cores (BF16 jobs with npad <= 128)
+bool tc_quality_ready(const gpunmf_job *j);
+gpunmf_status tc_quality(gpunmf_job *j);
 gpunmf_status tc_check(gpunmf_job *j);    // reads the kernels' error word (after a sync)
 void tc_destroy(gpunmf_job *j);
 }  // namespace gpunmf

@@ -743,6 +743,177 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
 }
 
 // ------------------------------------------------------------------------
+// quality on the tensor cores (BF16 jobs): sum V log10(WH + eps) - WH over all of V
+// (src/cuda/nmf/nmf_kernels_quality.cu:35, the value NMF::DetermineQualityImprovement samples),
+// with WH formed 128 x 128 at a time by tcgen05 from K-major BF16 copies of W (row-major) and H
+// (column-major) and never stored; V is streamed as BF16.  Warp 0 loads (TMA), warp 1 issues the
+// MMAs (double-buffered TMEM), warps 2-5 read their TMEM lane quarter and the V tile and add up
+// the terms, FP32 per tile row, FP64 across tiles.  Rows and columns beyond n and m read zeros
+// (TMA fill), which add 0 * log10(eps) - 0 = 0.
+// ------------------------------------------------------------------------
+constexpr int kQThreads = 192;
+constexpr int kQTile = 128;
+constexpr int kQVBytes = kQTile * kQTile * 2;
+
+struct QParams {
+    int tiles_i, tiles_u, nbox, npad, stages;
+    float eps;
+    double *partial;  // [grid]
+    int *err;
+};
+
+__global__ void __launch_bounds__(kQThreads, 1)
+    tc_quality_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const __grid_constant__ CUtensorMap tmV, QParams p) {
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
+    const int boxBytes = kQTile * kBlockK * 2;  // one 128 x 64 BF16 box (16 KB)
+    const int stageBytes = 2 * p.nbox * boxBytes + kQVBytes;
+    unsigned char *ring = reinterpret_cast<unsigned char *>(base);
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + p.stages * stageBytes);
+    uint64_t *empty = full + p.stages;
+    uint64_t *tfull = empty + p.stages;  // [2]
+    uint64_t *tempty = tfull + 2;        // [2]
+    uint64_t *mdone = tempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+    double *red = reinterpret_cast<double *>(tmem_slot + 2);  // [4], 8-byte aligned
+    auto sA = [&](int st) { return ring + st * stageBytes; };
+    auto sB = [&](int st) { return ring + st * stageBytes + p.nbox * boxBytes; };
+    auto sV = [&](int st) { return reinterpret_cast<const __nv_bfloat16 *>(ring + st * stageBytes + 2 * p.nbox * boxBytes); };
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int T = p.tiles_i * p.tiles_u;
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < p.stages; st++) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], 1 + 4);  // the MMAs (A, B) and the four epilogue warps (V)
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 4);
+        }
+        mbar_init(mdone, 1);
+        fence_mbar_init();
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
+        tma_prefetch_desc(&tmV);
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, 2 * kQTile);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int st = 0;
+            uint32_t ph = 0;
+            int armed[4] = {0, 0, 0, 0};
+            for (int t = blockIdx.x; t < T; t += gridDim.x) {
+                const int ti = t / p.tiles_u, tu = t % p.tiles_u;
+                if (!mbar_wait(&empty[st], ph ^ 1, p.err, kErrWaitEmpty)) break;
+                mbar_arrive_expect_tx(&full[st], (uint32_t)stageBytes);
+                for (int q = 0; q < p.nbox; q++) {
+                    tma_load_2d(sA(st) + q * boxBytes, &tmA, q * kBlockK, ti * kQTile, &full[st]);
+                    tma_load_2d(sB(st) + q * boxBytes, &tmB, q * kBlockK, tu * kQTile, &full[st]);
+                }
+                tma_load_2d(const_cast<__nv_bfloat16 *>(sV(st)), &tmV, ti * kQTile, tu * kQTile, &full[st]);
+                armed[st]++;
+                if (++st == p.stages) {
+                    st = 0;
+                    ph ^= 1;
+                }
+            }
+            if (*((volatile int *)p.err) != 0)
+                for (int k = 0; k < p.stages; k++)
+                    if (armed[k] > 0) mbar_wait_quiet(&full[k], (uint32_t)((armed[k] - 1) & 1));
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16_f32(kQTile, kQTile);
+            int st = 0, acc = 0;
+            uint32_t ph = 0, aph = 0;
+            for (int t = blockIdx.x; t < T; t += gridDim.x) {
+                if (!mbar_wait(&tempty[acc], aph ^ 1, p.err, kErrWaitTmemEmpty)) break;
+                if (!mbar_wait(&full[st], ph, p.err, kErrWaitFull)) break;
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(sA(st)), b0 = smem_u32(sB(st));
+                for (int k16 = 0; k16 < p.npad / 16; k16++) {
+                    const int q = k16 >> 2, w = (k16 & 3) * 32;
+                    tc_mma_f16(tmem + (uint32_t)(acc * kQTile), smem_desc(a0 + q * boxBytes + w, 16, 1024, 2),
+                               smem_desc(b0 + q * boxBytes + w, 16, 1024, 2), idesc, k16 > 0 ? 1u : 0u);
+                }
+                tc_commit(&empty[st]);
+                tc_commit(&tfull[acc]);
+                if (++st == p.stages) {
+                    st = 0;
+                    ph ^= 1;
+                }
+                if (++acc == 2) {
+                    acc = 0;
+                    aph ^= 1;
+                }
+            }
+            tc_commit(mdone);
+            mbar_wait_quiet(mdone, 0);
+        }
+    } else {
+        const int quarter = warp & 3;
+        const int i = quarter * 32 + lane;  // this thread's row of the tile (its TMEM lane)
+        const float eps = p.eps;
+        const float kLog10of2 = 0.30102999566398120f;
+        double dsum = 0.0;
+        int st = 0, acc = 0;
+        uint32_t ph = 0, aph = 0;
+        for (int t = blockIdx.x; t < T; t += gridDim.x) {
+            if (!warp_wait(&tfull[acc], aph, p.err, kErrWaitTmemFull)) break;
+            if (!warp_wait(&full[st], ph, p.err, kErrWaitFull)) break;  // the V tile of this stage
+            tc_fence_after();
+            const __nv_bfloat16 *v = sV(st);
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kQTile);
+            float part = 0.f;
+#pragma unroll 1
+            for (int c = 0; c < kQTile; c += 16) {
+                float sv[16];
+                tmem_ld16(taddr + c, sv);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const float vv = __bfloat162float(v[(c + j) * kQTile + i]);
+                    part += vv * (__log2f(sv[j] + eps) * kLog10of2) - sv[j];
+                }
+            }
+            dsum += (double)part;
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&tempty[acc]);
+                mbar_arrive(&empty[st]);
+            }
+            if (++st == p.stages) {
+                st = 0;
+                ph ^= 1;
+            }
+            if (++acc == 2) {
+                acc = 0;
+                aph ^= 1;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, off);
+        if (lane == 0) red[quarter] = dsum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) p.partial[blockIdx.x] = ((red[0] + red[1]) + red[2]) + red[3];
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 2 * kQTile);
+    }
+}
+
+// ------------------------------------------------------------------------
 // conversions
 // ------------------------------------------------------------------------
 // V (n x m FP32 column-major) -> Vb (ld ldv) and Vbt (= V^T, ld ldvt), 32x32 tiles through shared memory
@@ -1505,6 +1676,10 @@ struct TcState {
     float *P_h = nullptr, *P_w = nullptr;
     int *err = nullptr;
     float *G_w = nullptr, *G_h = nullptr;     // W'W and H H', npad x npad
+    // quality on the tensor cores: maps of Wr (W row-major), Hc (H column-major) and Vb
+    CUtensorMap tmQA, tmQB, tmQV;
+    gpunmf::QParams qp;
+    int qgrid = 0, qsmem = 0;
     float *GP_w = nullptr, *GP_h = nullptr;   // per-CTA Gram partials of the update kernels
     int gp_w_count = 0, gp_h_count = 0;
 };
@@ -1541,6 +1716,28 @@ static gpunmf_status make_map(CUtensorMap *m, const void *base, uint64_t d0, uin
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return GPUNMF_ERR_CUDA;
+    }
+    return GPUNMF_OK;
+}
+
+// 2-D BF16 tensor map without swizzle: box {box0, box1} (for tiles read by threads, not the MMA)
+static gpunmf_status make_map_plain(CUtensorMap *m, const void *base, uint64_t d0, uint64_t d1, uint64_t ld,
+                                    uint32_t box0, uint32_t box1) {
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return GPUNMF_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {d0, d1};
+    cuuint64_t strides[1] = {ld * 2};
+    cuuint32_t box[2] = {box0, box1};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (plain) failed (%d)", (int)r);
         return GPUNMF_ERR_CUDA;
     }
     return GPUNMF_OK;
@@ -1946,6 +2143,8 @@ static KlUpdParams kl_params_w(gpunmf_job *j, int update) {
     return u;
 }
 
+static gpunmf_status setup_quality(gpunmf_job *j);
+
 static gpunmf_status tc_create_kl(gpunmf_job *j) {
     TcState *t = j->tc;
     const int n = j->n, m = j->m, r = j->r;
@@ -1985,6 +2184,70 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
     if (st == GPUNMF_OK) st = make_map(&t->kw.tmB2, t->Hb, m, r, t->ldh, t->npad);
     if (st != GPUNMF_OK) return st;
     GPUNMF_CUDA_TRY(set_kl_smem_once());
+    return setup_quality(j);
+}
+
+// Quality on the tensor cores (npad <= 128): the maps, the launch shape and the shared memory.
+static gpunmf_status setup_quality(gpunmf_job *j) {
+    TcState *t = j->tc;
+    if (t->npad > 128) return GPUNMF_OK;  // the FP32 quality kernel serves larger ranks
+    const int n = j->n, m = j->m, r = j->r;
+    if (!t->Wr) {  // Euclidean jobs: the K-major copies are made when the quality is sampled
+        t->ldr = t->npad;
+        cudaError_t e = job_dev_alloc(j, (void **)&t->Wr, (size_t)n * t->ldr * 2);
+        if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hc, (size_t)m * t->ldr * 2);
+        if (e != cudaSuccess) {
+            set_error("quality buffers: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            return GPUNMF_ERR_NOMEM;
+        }
+    }
+    QParams &q = t->qp;
+    q.tiles_i = ceil_div(n, kQTile);
+    q.tiles_u = ceil_div(m, kQTile);
+    q.nbox = ceil_div(t->npad, kBlockK);
+    q.npad = t->npad;
+    q.eps = j->eps;
+    q.err = t->err;
+    const int stageBytes = 2 * q.nbox * kQTile * kBlockK * 2 + kQVBytes;
+    q.stages = std::min(3, (smem_optin() - 1024 - 256) / stageBytes);
+    t->qsmem = 1024 + q.stages * stageBytes + (2 * q.stages + 5) * 8 + 8 + 4 * 8 + 16;
+    t->qgrid = (int)std::min<long long>(num_sms(), (long long)q.tiles_i * q.tiles_u);
+    if (q.stages < 2 || (size_t)t->qgrid > j->red_cap) return GPUNMF_OK;  // not worth it here
+    gpunmf_status st = make_map(&t->tmQA, t->Wr, r, n, t->ldr, kQTile);
+    if (st == GPUNMF_OK) st = make_map(&t->tmQB, t->Hc, r, m, t->ldr, kQTile);
+    if (st == GPUNMF_OK) st = make_map_plain(&t->tmQV, t->Vb, n, m, t->ldv, kQTile, kQTile);
+    if (st != GPUNMF_OK) return st;
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(tc_quality_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin());
+    });
+    if (attr != cudaSuccess) {
+        set_error("cudaFuncSetAttribute (quality): %s", cudaGetErrorString(attr));
+        return GPUNMF_ERR_CUDA;
+    }
+    q.partial = j->red;
+    return GPUNMF_OK;
+}
+
+bool tc_quality_ready(const gpunmf_job *j) { return j->tc && j->tc->qp.partial != nullptr; }
+
+// The quality of the current factors into j->d_quality (float), as the FP32 path leaves it.
+gpunmf_status tc_quality(gpunmf_job *j) {
+    TcState *t = j->tc;
+    cudaStream_t s = j->stream;
+    if (!rule_is_kl(j->rule)) {  // Euclidean jobs keep only Wb / Hb current: make the K-major copies
+        convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->n * t->ldr, 256)), 256, 0, s>>>(
+            j->W, j->n, j->r, j->n, true, t->Wr, t->ldr);
+        convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->m * t->ldr, 256)), 256, 0, s>>>(
+            j->H, j->m, j->r, 0, false, t->Hc, t->ldr);
+        j->launches += 2;
+    }
+    tc_quality_kernel<<<t->qgrid, kQThreads, t->qsmem, s>>>(t->tmQA, t->tmQB, t->tmQV, t->qp);
+    GPUNMF_CUDA_TRY(cudaGetLastError());
+    GPUNMF_CUDA_TRY(finalize_partials(j->red, t->qgrid, 1, 0, j->d_quality, nullptr, s));
+    j->launches += 2;
     return GPUNMF_OK;
 }
 
@@ -2097,7 +2360,7 @@ gpunmf_status tc_create(gpunmf_job *j) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return GPUNMF_ERR_CUDA;
     }
-    return GPUNMF_OK;
+    return setup_quality(j);
 }
 
 gpunmf_status tc_prepare(gpunmf_job *j) {

@@ -118,3 +118,25 @@ def test_bf16_quality_path(gpu):
             nmf.DoIteration()
         q = nmf.QualityImprovement()
     assert np.isfinite(q) and q != 1.0
+
+
+@pytest.mark.parametrize("rule,shape", [(0, (2048, 1536, 64)), (0, (1000, 777, 20)), (1, (1024, 2048, 64)),
+                                        (0, (300, 4100, 128))])
+def test_bf16_quality_tracks_fp32(gpu, rule, shape):
+    """BF16 jobs sample the quality on the tensor cores (W H from the BF16 factors, V as BF16): the
+    lagged improvements (nmf_base.h:70-89) follow the FP32 job's over the first iterations."""
+    n, m, r = shape
+    V = inputs.lowrank_gamma(n, m, min(r, 16), 2.0, 0.5, seed=23)
+    W, H = inputs.factors(24, n, m, r)
+    seqs = {}
+    for prec in ("fp32", "bf16"):
+        with gpu.make(rule, V, W, H, eps=1e-9, precision=prec) as nmf:
+            d = []
+            for _ in range(8):
+                nmf.DoIteration()
+                d.append(nmf.QualityImprovement())
+            seqs[prec] = np.array(d, dtype=np.float64)
+    a, b = seqs["fp32"], seqs["bf16"]
+    assert a[0] == b[0] == 1.0 and a[1] == b[1] == 1.0      # no improvement before the third sample
+    scale = np.abs(a[2:]).max()
+    assert np.abs(a[2:] - b[2:]).max() <= 2e-2 * scale, (a, b)
