@@ -47,8 +47,9 @@ METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from the committed ncu
 # captures of this workload (one --set full capture per precision, see the profiles
-# directory): tc_gemm_sk_kernel 143.77 MB + 3.27 MB; gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
-NCU_TRAFFIC_PER_LAUNCH = {"bf16": 147.04e6, "fp32": 276.09e6}
+# directory): tc_gemm_sk_kernel<64> with the update fused in 137.82 MB + 3.61 MB;
+# gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
+NCU_TRAFFIC_PER_LAUNCH = {"bf16": 141.43e6, "fp32": 276.09e6}
 
 
 def parse():
@@ -272,14 +273,22 @@ def run_ours(args, rank, world, local, dist):
     # roofline of the dominant kernel (the V-streaming product)
     hbm, _, src = peaks()
     vbytes = 2 if precision == "bf16" else 4
-    per_launch_bytes = n * m * vbytes + (n * r + r * m) * vbytes + (r * m if precision != "bf16" else 0) * 4
+    if precision == "bf16":
+        # one half-step kernel: V (BF16) once, the other factor's BF16 copy once, and the updated
+        # factor read (FP32), written (FP32) and written again as BF16
+        per_launch_bytes = n * m * 2 + n * r * 2 + m * r * (4 + 4 + 2)
+    else:
+        # the W'V product: V, W and the FP32 partial products of H's shape
+        per_launch_bytes = n * m * 4 + (n * r + r * m) * 4 + r * m * 4
     kl = max(1, t["kernel_launches"])
     avg_ms = t["kernel_ms"] / kl
     achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
     traffic = NCU_TRAFFIC_PER_LAUNCH.get(precision)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": src,
-                "kernel": "V-streaming product (W'V / VH')", "avg_launch_ms": round(avg_ms, 5),
+                "kernel": ("half-step kernel: V-streaming product with the update fused (tc_gemm_sk_kernel)"
+                           if precision == "bf16" else "V-streaming product W'V (gemm_f32_kernel)"),
+                "avg_launch_ms": round(avg_ms, 5),
                 "algorithmic_bytes_per_launch": per_launch_bytes}
 
     out = {"metric": METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": world, "steps": args.steps,

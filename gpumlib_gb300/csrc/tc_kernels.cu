@@ -746,12 +746,16 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
 // quality on the tensor cores (BF16 jobs): sum V log10(WH + eps) - WH over all of V
 // (src/cuda/nmf/nmf_kernels_quality.cu:35, the value NMF::DetermineQualityImprovement samples),
 // with WH formed 128 x 128 at a time by tcgen05 from K-major BF16 copies of W (row-major) and H
-// (column-major) and never stored; V is streamed as BF16.  Warp 0 loads (TMA), warp 1 issues the
-// MMAs (double-buffered TMEM), warps 2-5 read their TMEM lane quarter and the V tile and add up
-// the terms, FP32 per tile row, FP64 across tiles.  Rows and columns beyond n and m read zeros
-// (TMA fill), which add 0 * log10(eps) - 0 = 0.
+// (column-major) and never stored; V is streamed as BF16 from its transposed copy, two 128-byte
+// swizzled boxes per tile, so a thread reads its row's values 16 bytes at a time without bank
+// conflicts.  Warp 0 loads (TMA), warp 1 issues the
+// MMAs (double-buffered TMEM), sixteen warps (four per TMEM lane quarter, 32 columns each) read
+// the accumulator and the V tile and add up sum v log2(s + eps) and sum s separately, FP32 per
+// tile row, FP64 across tiles; quality = log10(2) * the first - the second.  Rows and columns
+// beyond n and m read zeros (TMA fill), which add 0.
 // ------------------------------------------------------------------------
-constexpr int kQThreads = 192;
+constexpr int kQEpiWarps = 16;
+constexpr int kQThreads = 64 + 32 * kQEpiWarps;
 constexpr int kQTile = 128;
 constexpr int kQVBytes = kQTile * kQTile * 2;
 
@@ -775,7 +779,7 @@ __global__ void __launch_bounds__(kQThreads, 1)
     uint64_t *tempty = tfull + 2;        // [2]
     uint64_t *mdone = tempty + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
-    double *red = reinterpret_cast<double *>(tmem_slot + 2);  // [4], 8-byte aligned
+    double *red = reinterpret_cast<double *>(tmem_slot + 2);  // [2][kQEpiWarps], 8-byte aligned
     auto sA = [&](int st) { return ring + st * stageBytes; };
     auto sB = [&](int st) { return ring + st * stageBytes + p.nbox * boxBytes; };
     auto sV = [&](int st) { return reinterpret_cast<const __nv_bfloat16 *>(ring + st * stageBytes + 2 * p.nbox * boxBytes); };
@@ -785,11 +789,11 @@ __global__ void __launch_bounds__(kQThreads, 1)
     if (threadIdx.x == 0) {
         for (int st = 0; st < p.stages; st++) {
             mbar_init(&full[st], 1);
-            mbar_init(&empty[st], 1 + 4);  // the MMAs (A, B) and the four epilogue warps (V)
+            mbar_init(&empty[st], 1 + kQEpiWarps);  // the MMAs (A, B) and the epilogue warps (V)
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(&tfull[a], 1);
-            mbar_init(&tempty[a], 4);
+            mbar_init(&tempty[a], kQEpiWarps);
         }
         mbar_init(mdone, 1);
         fence_mbar_init();
@@ -819,7 +823,9 @@ __global__ void __launch_bounds__(kQThreads, 1)
                     tma_load_2d(sA(st) + q * boxBytes, &tmA, q * kBlockK, ti * kQTile, &full[st]);
                     tma_load_2d(sB(st) + q * boxBytes, &tmB, q * kBlockK, tu * kQTile, &full[st]);
                 }
-                tma_load_2d(const_cast<__nv_bfloat16 *>(sV(st)), &tmV, ti * kQTile, tu * kQTile, &full[st]);
+                for (int q = 0; q < 2; q++)  // V' tile: rows i, 64 columns u per box
+                    tma_load_2d(const_cast<__nv_bfloat16 *>(sV(st)) + q * (kQTile * 64), &tmV, tu * kQTile + q * 64,
+                                ti * kQTile, &full[st]);
                 armed[st]++;
                 if (++st == p.stages) {
                     st = 0;
@@ -860,11 +866,11 @@ __global__ void __launch_bounds__(kQThreads, 1)
             mbar_wait_quiet(mdone, 0);
         }
     } else {
-        const int quarter = warp & 3;
-        const int i = quarter * 32 + lane;  // this thread's row of the tile (its TMEM lane)
+        const int quarter = warp & 3;          // TMEM lanes this warp may read
+        const int c0 = ((warp - 2) >> 2) * 32; // its 32 columns of the tile
+        const int i = quarter * 32 + lane;     // this thread's row of the tile (its TMEM lane)
         const float eps = p.eps;
-        const float kLog10of2 = 0.30102999566398120f;
-        double dsum = 0.0;
+        double dlog = 0.0, ds = 0.0;
         int st = 0, acc = 0;
         uint32_t ph = 0, aph = 0;
         for (int t = blockIdx.x; t < T; t += gridDim.x) {
@@ -872,20 +878,40 @@ __global__ void __launch_bounds__(kQThreads, 1)
             if (!warp_wait(&full[st], ph, p.err, kErrWaitFull)) break;  // the V tile of this stage
             tc_fence_after();
             const __nv_bfloat16 *v = sV(st);
-            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kQTile);
-            float part = 0.f;
-#pragma unroll 1
-            for (int c = 0; c < kQTile; c += 16) {
-                float sv[16];
-                tmem_ld16(taddr + c, sv);
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kQTile + c0);
+            float sv[32];
+            {
+                float a[16], b[16];
+                tmem_ld16(taddr, a);
+                tmem_ld16(taddr + 16, b);
                 tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
-                    const float vv = __bfloat162float(v[(c + j) * kQTile + i]);
-                    part += vv * (__log2f(sv[j] + eps) * kLog10of2) - sv[j];
+                    sv[j] = a[j];
+                    sv[16 + j] = b[j];
                 }
             }
-            dsum += (double)part;
+            // this row's 32 values of V: 4 chunks of 8 in the 128-byte swizzled row i of box c0 / 64
+            const unsigned char *vrow =
+                reinterpret_cast<const unsigned char *>(v + (c0 >> 6) * (kQTile * 64)) + i * 128;
+            float plog = 0.f, ps = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int chunk = (((c0 & 63) >> 3) + k) ^ (i & 7);
+                const uint4 raw = *reinterpret_cast<const uint4 *>(vrow + chunk * 16);
+                const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&raw);
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float2 vv = __bfloat1622float2(h2[e]);
+                    const int j = 8 * k + 2 * e;
+                    plog = fmaf(vv.x, __log2f(sv[j] + eps), plog);
+                    plog = fmaf(vv.y, __log2f(sv[j + 1] + eps), plog);
+                    ps += sv[j];
+                    ps += sv[j + 1];
+                }
+            }
+            dlog += (double)plog;
+            ds += (double)ps;
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -902,11 +928,24 @@ __global__ void __launch_bounds__(kQThreads, 1)
             }
         }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, off);
-        if (lane == 0) red[quarter] = dsum;
+        for (int off = 16; off > 0; off >>= 1) {
+            dlog += __shfl_down_sync(0xffffffffu, dlog, off);
+            ds += __shfl_down_sync(0xffffffffu, ds, off);
+        }
+        if (lane == 0) {
+            red[warp - 2] = dlog;
+            red[kQEpiWarps + warp - 2] = ds;
+        }
     }
     __syncthreads();
-    if (threadIdx.x == 0) p.partial[blockIdx.x] = ((red[0] + red[1]) + red[2]) + red[3];
+    if (threadIdx.x == 0) {
+        double l = 0.0, sm = 0.0;
+        for (int w = 0; w < kQEpiWarps; w++) {
+            l += red[w];
+            sm += red[kQEpiWarps + w];
+        }
+        p.partial[blockIdx.x] = 0.30102999566398120 * l - sm;  // log10(x) = log2(x) log10(2)
+    }
     if (warp == 0) {
         tc_fence_after();
         tmem_dealloc(tmem, 2 * kQTile);
@@ -1721,28 +1760,6 @@ static gpunmf_status make_map(CUtensorMap *m, const void *base, uint64_t d0, uin
     return GPUNMF_OK;
 }
 
-// 2-D BF16 tensor map without swizzle: box {box0, box1} (for tiles read by threads, not the MMA)
-static gpunmf_status make_map_plain(CUtensorMap *m, const void *base, uint64_t d0, uint64_t d1, uint64_t ld,
-                                    uint32_t box0, uint32_t box1) {
-    auto fn = encode_fn();
-    if (!fn) {
-        set_error("cuTensorMapEncodeTiled is not available from the driver");
-        return GPUNMF_ERR_CUDA;
-    }
-    cuuint64_t dims[2] = {d0, d1};
-    cuuint64_t strides[1] = {ld * 2};
-    cuuint32_t box[2] = {box0, box1};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("cuTensorMapEncodeTiled (plain) failed (%d)", (int)r);
-        return GPUNMF_ERR_CUDA;
-    }
-    return GPUNMF_OK;
-}
-
 static int num_sms() {
     static int sms = 0;
     if (!sms) {
@@ -2211,12 +2228,12 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
     q.err = t->err;
     const int stageBytes = 2 * q.nbox * kQTile * kBlockK * 2 + kQVBytes;
     q.stages = std::min(3, (smem_optin() - 1024 - 256) / stageBytes);
-    t->qsmem = 1024 + q.stages * stageBytes + (2 * q.stages + 5) * 8 + 8 + 4 * 8 + 16;
+    t->qsmem = 1024 + q.stages * stageBytes + (2 * q.stages + 5) * 8 + 8 + 2 * kQEpiWarps * 8 + 16;
     t->qgrid = (int)std::min<long long>(num_sms(), (long long)q.tiles_i * q.tiles_u);
     if (q.stages < 2 || (size_t)t->qgrid > j->red_cap) return GPUNMF_OK;  // not worth it here
     gpunmf_status st = make_map(&t->tmQA, t->Wr, r, n, t->ldr, kQTile);
     if (st == GPUNMF_OK) st = make_map(&t->tmQB, t->Hc, r, m, t->ldr, kQTile);
-    if (st == GPUNMF_OK) st = make_map_plain(&t->tmQV, t->Vb, n, m, t->ldv, kQTile, kQTile);
+    if (st == GPUNMF_OK) st = make_map(&t->tmQV, t->Vbt, m, n, t->ldvt, kQTile);  // V': {u, i}, box {64, 128}
     if (st != GPUNMF_OK) return st;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
