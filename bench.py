@@ -193,8 +193,9 @@ def euclid_madds(n, m, r):
     return 2 * n * m * r + r * r * n + r * r * m + r * r * m + n * r * r + n * r * r
 
 
-def cpu_reference_steps(V, W, H, r, steps, warmup, slice_cols=128):
-    """Time the reference CPU iteration on a column slice; returns (iters/s full-size, info)."""
+def cpu_reference_steps(V, W, H, r, steps, warmup, slice_cols=128, min_seconds=0.0):
+    """Time the reference CPU iteration on a column slice (at least `steps` iterations and, if given,
+    at least min_seconds of CPU work); returns (iters/s full-size, info)."""
     import oracle
     n, m = V.shape
     mc = min(slice_cols, m)
@@ -216,9 +217,12 @@ def cpu_reference_steps(V, W, H, r, steps, warmup, slice_cols=128):
     for _ in range(warmup):
         one()
     t0 = time.perf_counter()
-    for _ in range(steps):
+    done = 0
+    while done < steps or time.perf_counter() - t0 < min_seconds:
         one()
+        done += 1
     dt = time.perf_counter() - t0
+    steps = done
     scale = euclid_madds(n, mc, r) / euclid_madds(n, m, r)
     ips = steps * scale / dt
     info = {"kind": kind, "cores": 1 if use_ref else threads,
@@ -319,7 +323,8 @@ def run_ours(args, rank, world, local, dist):
             out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 3)
 
     if rank == 0 and not args.no_cpu_baseline:
-        ips, info = cpu_reference_steps(V, W, H, r, steps=3, warmup=1)
+        # a bounded sample of about 10 s of host-core work: iterations of a 1024-column slice
+        ips, info = cpu_reference_steps(V, W, H, r, steps=3, warmup=1, slice_cols=1024, min_seconds=10.0)
         out["cpu_baseline"] = {"value": ips, "unit": "iters/s", **info}
     return out
 
