@@ -65,11 +65,12 @@ struct SkParams {
     int gram_count;
     int gram_entries;
     // fused update (kernel template FNP > 0).  Every CTA owns a contiguous slice of the rows of the
-    // factor X it updates.  While its tensor pipe streams V, two worker warps copy the old rows and
-    // the Gram of the other factor into shared memory and form the denominators X G; after the
+    // factor X it updates.  While its tensor pipe streams V, two worker warps assemble the Gram of
+    // the other factor from that factor's per-CTA partials (each CTA sums a slice, then all copy
+    // the whole), copy the old rows into shared memory and form the denominators X G; after the
     // GEMM, the whole CTA waits until the tiles its rows belong to have all their partial
-    // products, sums them, writes the new rows, and reduces the Gram of the new factor (two levels,
-    // last arrivals, fixed order) for the next kernel.
+    // products, sums them, writes the new rows, and leaves its rows' Gram partial for the next
+    // kernel.
     float *X;                          // FP32 factor updated: H (r x m) or W (n x r), column-major
     __nv_bfloat16 *Xb;                 // its BF16 copy (Hb row-major / Wb column-major, ld ldb)
     long long ldb;
@@ -78,14 +79,12 @@ struct SkParams {
     const int *slot_ptr, *slot_list;   // each tile's slots in K order
     int *tile_cnt, *tile_rd;           // per tile: partial products arrived, readers done (reset by the last)
     const int *tile_readers;           // per tile: how many row chunks read it
-    const float *G_in;                 // npad^2: the complete Gram of the other factor
-    float *G_out;                      // npad^2: the complete Gram of the new factor
-    float *gp, *gg;                    // [grid][npad^2] per-CTA partials, [groups][npad^2] group sums
-    int *grp_cnt, *all_cnt;            // arrivals per group of 8 CTAs; group sums out, finishers done
-    int ngroups;
+    const float *gin_parts;            // [gin_count][npad^2] the other factor's per-CTA Gram partials
+    int gin_count;
+    float *G_full;                     // npad^2: the complete Gram of the other factor, assembled here
+    int *red_cnt;                      // [2]: Gram slices published, CTAs done reading (last resets)
+    float *gp;                         // [grid][npad^2] this kernel's per-CTA partials of the new factor
 };
-
-constexpr int kGramGroup = 8;  // tile Gram partials reduced per group, then the group sums
 
 extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
 
@@ -251,29 +250,74 @@ __device__ __forceinline__ void chunk_denominators(const float *sX, float *sG, i
                 make_float4(den[k][4 * cc], den[k][4 * cc + 1], den[k][4 * cc + 2], den[k][4 * cc + 3]);
 }
 
-// Prologue of the fused update (the two worker warps, while V streams): the old rows of this
-// CTA's first chunk and the complete Gram of the other factor copied into shared memory (all
-// copies in flight at once), then the chunk's denominators (left in sG as sD).
+// Entry u of the upper triangle of an NP x NP Gram, column by column: (i, k) with i <= k,
+// u = k (k + 1) / 2 + i.
+__device__ __forceinline__ int2 tri_entry(int u) {
+    int k = (int)((sqrtf(8.f * (float)u + 1.f) - 1.f) * 0.5f);
+    if ((k + 1) * (k + 2) / 2 <= u) k++;
+    if (k * (k + 1) / 2 > u) k--;
+    return make_int2(u - k * (k + 1) / 2, k);
+}
+
+// Prologue of the fused update (the two worker warps, while V streams).  The complete Gram of the
+// other factor is assembled from that factor's per-CTA partials: this CTA sums a slice of the
+// upper triangle over the partials in their order (so the result does not depend on which CTA
+// does it) and writes both mirror entries; once every CTA has published its slice (grid-wide
+// counter, bounded wait) the whole Gram is copied in.  Meanwhile the old rows of this CTA's first
+// chunk are copied in; then the chunk's denominators (left in sG as sD).  All copies are
+// cp.async, so they are in flight together while the stream holds HBM.
 template <int NP>
-__device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float *sG, float *sX) {
-    constexpr int E = NP * NP;
-    const int c = blockIdx.x, G = gridDim.x;
+__device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float *sG, float *sX, int *sflag) {
+    constexpr int E = NP * NP, U = NP * (NP + 1) / 2, CAP = fused_gram_floats(NP);
+    const int c = blockIdx.x, G = gridDim.x, P = pr.gin_count;
     const long long x0 = (long long)c * pr.rows_valid / G, x1 = (long long)(c + 1) * pr.rows_valid / G;
     stage_rows_async<NP, 64>(pr.X, pr.is_w, pr.rows_valid, pr.r, x0, (int)min(64LL, x1 - x0), sX, wt,
                              (pr.r & 3) == 0);
-    for (int k = wt; k < E / 4; k += 64) cp_async16(sG + 4 * k, pr.G_in + 4 * k, true);
+    const int u0 = (int)((long long)c * U / G), u1 = (int)((long long)(c + 1) * U / G);
+    const int per = CAP / P;  // entries whose partials fit the staging area at once (P <= 152)
+    for (int ub = u0; ub < u1; ub += per) {
+        const int nb = min(per, u1 - ub);
+        for (int k = wt; k < nb * P; k += 64) {
+            const int j = k / P, q = k - j * P;
+            const int2 ik = tri_entry(ub + j);
+            cp_async4(sG + k, pr.gin_parts + (size_t)q * E + ik.x * NP + ik.y, true);
+        }
+        cp_async_commit();
+        cp_async_wait_all();
+        wk_bar();
+        for (int j = wt; j < nb; j += 64) {
+            float sum = 0.f;
+            for (int q = 0; q < P; q++) sum += sG[j * P + q];
+            const int2 ik = tri_entry(ub + j);
+            pr.G_full[ik.x * NP + ik.y] = sum;
+            pr.G_full[ik.y * NP + ik.x] = sum;
+        }
+        wk_bar();
+    }
+    cp_async_wait_all();
+    __threadfence();
+    wk_bar();
+    if (wt == 0) {
+        atomicAdd(pr.red_cnt, 1);
+        sflag[2] = flag_wait_ge(pr.red_cnt, G, pr.err, kErrWaitGram) ? 1 : 0;
+    }
+    wk_bar();
+    if (!sflag[2]) return;  // the error word is set: the tail is skipped
+    for (int k = wt; k < E / 4; k += 64) cp_async16(sG + 4 * k, pr.G_full + 4 * k, true);
     cp_async_commit();
     cp_async_wait_all();
     wk_bar();
+    if (wt == 0 && atomicAdd(pr.red_cnt + 1, 1) == G - 1) {  // every CTA is past the wait: reset
+        pr.red_cnt[1] = 0;
+        atomicExch(pr.red_cnt, 0);
+    }
     chunk_denominators<NP, 64>(sX, sG, wt, wk_bar);
 }
 
 // Tail of the fused update (all 256 threads, after the GEMM): per chunk of this CTA's rows, wait
 // until the chunk's tiles have all their partial products, sum them in K order,
 // X_new = X num / (den + eps) or max(0, X + X / den (num - den)), write X and its BF16 copy and
-// add the new rows to this CTA's Gram partial; then the two-level reduction of the partials into
-// the complete Gram of the new factor (the last CTA of a group of 8 sums the group, the last group
-// sums the groups, each in a fixed order, so the result does not depend on arrival order).
+// add the new rows to this CTA's Gram partial, which the next kernel sums with the other CTAs'.
 template <int NP>
 __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *sG, float *sX, int *sflag, int *sSl) {
     constexpr int NT = 256;
@@ -307,7 +351,7 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             __syncthreads();
             stage_rows<NP, NT>(X, is_w, rows, r, xb, nr, sX, tid);
             for (int k = tid; k < E / 4; k += NT)
-                reinterpret_cast<float4 *>(sG)[k] = __ldcg(reinterpret_cast<const float4 *>(pr.G_in) + k);
+                reinterpret_cast<float4 *>(sG)[k] = __ldcg(reinterpret_cast<const float4 *>(pr.G_full) + k);
             __syncthreads();
             chunk_denominators<NP, NT>(sX, sG, tid, bar);
         }
@@ -436,66 +480,6 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
     for (int i = 0; i < GB; i++)
 #pragma unroll
         for (int k = 0; k < GB; k++) gpc[(ga0 + i) * NP + gb0 + k] = gacc[i][k];
-    // two-level reduction of the CTAs' partials into G_out
-    __threadfence();
-    __syncthreads();
-    const int g = c / kGramGroup, gsize = min(kGramGroup, G - g * kGramGroup);
-    if (tid == 0) *sflag = atomicAdd(pr.grp_cnt + g, 1) == gsize - 1 ? 1 : 0;
-    __syncthreads();
-    if (*sflag) {
-        __threadfence();
-        constexpr int EPT = E / NT;
-        const float *src = pr.gp + (size_t)g * kGramGroup * E;
-        float sum[EPT];
-#pragma unroll
-        for (int k = 0; k < EPT; k++) sum[k] = 0.f;
-        {
-            float v[kGramGroup][EPT];
-#pragma unroll
-            for (int q = 0; q < kGramGroup; q++)
-#pragma unroll
-                for (int k = 0; k < EPT; k++) v[q][k] = q < gsize ? __ldcg(src + (size_t)q * E + tid + k * NT) : 0.f;
-#pragma unroll
-            for (int q = 0; q < kGramGroup; q++)
-#pragma unroll
-                for (int k = 0; k < EPT; k++)
-                    if (q < gsize) sum[k] += v[q][k];
-        }
-#pragma unroll
-        for (int k = 0; k < EPT; k++) pr.gg[(size_t)g * E + tid + k * NT] = sum[k];
-        __threadfence();
-        __syncthreads();
-        // second level, spread over the group finishers: each waits until every group sum is out,
-        // then sums its slice of the entries over the groups in order
-        const int ng = pr.ngroups;
-        if (tid == 0) {
-            pr.grp_cnt[g] = 0;
-            atomicAdd(pr.all_cnt, 1);
-            *sflag = flag_wait_ge(pr.all_cnt, ng, err, kErrWaitGram) ? 1 : 0;
-        }
-        __syncthreads();
-        if (*sflag) {
-            __threadfence();
-            const int e0 = (int)((long long)g * E / ng), e1 = (int)((long long)(g + 1) * E / ng);
-            for (int e = e0 + tid; e < e1; e += NT) {
-                float v[32];
-                float acc = 0.f;
-                for (int q0 = 0; q0 < ng; q0 += 32) {
-#pragma unroll
-                    for (int q = 0; q < 32; q++) v[q] = q0 + q < ng ? __ldcg(pr.gg + (size_t)(q0 + q) * E + e) : 0.f;
-#pragma unroll
-                    for (int q = 0; q < 32; q++)
-                        if (q0 + q < ng) acc += v[q];
-                }
-                pr.G_out[e] = acc;
-            }
-            __syncthreads();
-            if (tid == 0 && atomicAdd(pr.all_cnt + 1, 1) == ng - 1) {  // the last finisher resets
-                pr.all_cnt[1] = 0;
-                atomicExch(pr.all_cnt, 0);
-            }
-        }
-    }
 }
 
 // Gram partials of a factor for the first fused kernel: CTA c over rows [c*rows/G, (c+1)*rows/G),
@@ -727,7 +711,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             b = e;
         }
     } else if constexpr (FNP > 0) {
-        fused_prologue<FNP>(p, threadIdx.x - kGemmThreads, sG, sX);  // warps 6 and 7
+        fused_prologue<FNP>(p, threadIdx.x - kGemmThreads, sG, sX, sflag);  // warps 6 and 7
     }
     __syncthreads();
     if constexpr (FNP > 0) {
@@ -1691,8 +1675,8 @@ struct TcGemm {
     int fnp = 0;  // fused update rank (kernel template argument), 0 = separate update kernel
     int *slot_ptr = nullptr, *slot_list = nullptr;
     int *tile_slots = nullptr;
-    int *counters = nullptr;  // [tiles] tile arrivals, [groups] group arrivals, [1] total
-    float *grams = nullptr;   // [tiles + groups][npad^2] tile Gram partials and group sums
+    int *counters = nullptr;  // [tiles] arrivals, [tiles] readers done, [tiles] readers, [2] Gram assembly
+    float *grams = nullptr;   // [grid][npad^2] per-CTA Gram partials of the factor this GEMM updates
 };
 
 struct KlGemm {
@@ -1869,8 +1853,8 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     g.p.slot_ptr = g.slot_ptr;
     g.p.slot_list = g.slot_list;
     if (fnp) {
-        // per tile: arrivals, readers done, readers expected; the Gram slice counters; per CTA the
-        // Gram partial of its new rows
+        // per tile: arrivals, readers done, readers expected; the Gram assembly counters; per CTA
+        // the Gram partial of its new rows
         const int G = g.grid;
         std::vector<int> readers(tiles, 0);
         for (int c = 0; c < G; c++) {
@@ -1880,13 +1864,12 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
                 for (long long t = xb / kTileM; t <= (xe - 1) / kTileM; t++) readers[t]++;
             }
         }
-        const int groups = ceil_div(G, kGramGroup);
-        const size_t nc = (size_t)3 * tiles + groups + 2;
+        const size_t nc = (size_t)3 * tiles + 2;
         e = job_dev_alloc(j, (void **)&g.counters, nc * sizeof(int));
         if (e == cudaSuccess) e = cudaMemsetAsync(g.counters, 0, nc * sizeof(int), j->stream);
         if (e == cudaSuccess) e = job_h2d(j, g.counters + 2 * tiles, readers.data(), tiles * sizeof(int));
         if (e == cudaSuccess)
-            e = job_dev_alloc(j, (void **)&g.grams, (size_t)(G + groups) * fnp * fnp * sizeof(float));
+            e = job_dev_alloc(j, (void **)&g.grams, (size_t)G * fnp * fnp * sizeof(float));
         if (e != cudaSuccess) {
             set_error("fused-update workspace allocation failed: %s", cudaGetErrorString(e));
             cudaGetLastError();
@@ -1895,11 +1878,8 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
         g.p.tile_cnt = g.counters;
         g.p.tile_rd = g.counters + tiles;
         g.p.tile_readers = g.counters + 2 * tiles;
-        g.p.grp_cnt = g.counters + 3 * tiles;
-        g.p.all_cnt = g.p.grp_cnt + groups;
+        g.p.red_cnt = g.counters + 3 * tiles;
         g.p.gp = g.grams;
-        g.p.gg = g.grams + (size_t)G * fnp * fnp;
-        g.p.ngroups = groups;
     }
     return GPUNMF_OK;
 }
@@ -1927,8 +1907,8 @@ static int fused_rank(int npad) { return (npad == 32 || npad == 64) ? npad : 0; 
 static size_t fused_bytes(int rows, int npad) {
     const int np = fused_rank(npad);
     if (!np) return 0;
-    const int tiles = ceil_div(rows, kTileM), groups = ceil_div(kNumSMsGB300, kGramGroup);
-    return (size_t)(3 * tiles + groups + 2) * sizeof(int) + (size_t)(kNumSMsGB300 + groups) * np * np * sizeof(float);
+    const int tiles = ceil_div(rows, kTileM);
+    return (size_t)(3 * tiles + 2) * sizeof(int) + (size_t)kNumSMsGB300 * np * np * sizeof(float);
 }
 
 static size_t gemm_partial_bytes(int rows, int K, int npad) {
@@ -2339,18 +2319,17 @@ gpunmf_status tc_create(gpunmf_job *j) {
     if (st == GPUNMF_OK) st = setup_gemm(j, t->gw, n, m, t->npad, &t->P_w, t->err, fnp);
     if (st != GPUNMF_OK) return st;
     if (fnp) {
-        // each GEMM updates its factor itself and leaves that factor's complete Gram for the other
-        // each GEMM takes the Gram the other left (W'W for the H-step, H H' for the W-step) and
-        // leaves the Gram of the factor it updates
+        // each GEMM updates its factor itself and leaves per-CTA Gram partials of it; the other
+        // GEMM assembles the complete Gram from them (W'W for the H-step, H H' for the W-step)
         auto fill = [&](SkParams &q, float *X, __nv_bfloat16 *Xb, long long ldb, int is_w, int rows,
-                        const float *G_in, float *G_out) {
+                        const TcGemm &other, float *G_full) {
             q.X = X; q.Xb = Xb; q.ldb = ldb; q.is_w = is_w; q.rows_valid = rows; q.r = r;
             q.additive = rule_is_additive(j->rule) ? 1 : 0; q.eps = j->eps;
-            q.G_in = G_in; q.G_out = G_out;
+            q.gin_parts = other.grams; q.gin_count = other.grid; q.G_full = G_full;
             q.gram_out = nullptr;
         };
-        fill(t->gh.p, j->H, t->Hb, t->ldh, 0, m, t->G_w, t->G_h);   // H-step: den = W'W H
-        fill(t->gw.p, j->W, t->Wb, t->ldw, 1, n, t->G_h, t->G_w);   // W-step: den = W H H'
+        fill(t->gh.p, j->H, t->Hb, t->ldh, 0, m, t->gw, t->G_w);   // H-step: den = W'W H
+        fill(t->gw.p, j->W, t->Wb, t->ldw, 1, n, t->gh, t->G_h);   // W-step: den = W H H'
     } else {
         // the H-step GEMM finishes W'W from the W-step update's partials, and vice versa
         t->gh.p.gram_partials = t->GP_w;
@@ -2401,20 +2380,17 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
         return GPUNMF_OK;
     }
     if (t->gh.fnp) {
-        // the complete Gram of the initial W for the first H-step (and of the fixed H for a rule
-        // without an H step): per-CTA partials, then their sum
-        const long long E = (long long)t->npad * t->npad;
-        const int G = t->gw.grid;
+        // the Gram partials of the initial W, where the W-step would leave them, for the first
+        // H-step (and of the fixed H, where the H-step would leave them, for a rule without an
+        // H step), over the same row partitions
         switch (t->gh.fnp) {
 #define GP(NP)                                                                                          \
     case NP:                                                                                            \
-        gram_partials_kernel<NP><<<G, 64, 0, s>>>(j->W, 1, j->n, j->r, t->gw.grams);                   \
+        gram_partials_kernel<NP><<<t->gw.grid, 64, 0, s>>>(j->W, 1, j->n, j->r, t->gw.grams);          \
         GPUNMF_CUDA_TRY(cudaGetLastError());                                                            \
-        GPUNMF_CUDA_TRY(sum_partials(t->G_w, t->gw.grams, G, E, s));                                   \
         if (j->rule == GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H) {                                             \
-            gram_partials_kernel<NP><<<G, 64, 0, s>>>(j->H, 0, j->m, j->r, t->gw.grams);               \
+            gram_partials_kernel<NP><<<t->gh.grid, 64, 0, s>>>(j->H, 0, j->m, j->r, t->gh.grams);      \
             GPUNMF_CUDA_TRY(cudaGetLastError());                                                        \
-            GPUNMF_CUDA_TRY(sum_partials(t->G_h, t->gw.grams, G, E, s));                               \
         }                                                                                               \
         break;
             GP(32) GP(64)
