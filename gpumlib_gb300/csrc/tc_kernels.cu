@@ -1212,22 +1212,30 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
 // ========================================================================
 // KL rule (nmf_multiplicative_divergence.cpp:29-50, nmf_kernels.cu:247-341):
 // fused  S = (W H) block -> R = V / (S + eps) -> numerator += R x factor,
-// never materialising W H.  Per 128-row output tile and 64-wide K block:
-//   MMA1  D1[128 x 64]  = A1[128 x r] B1[64 x r]^T     (S for the block, in TMEM)
-//   epilogue warps: R = V / (D1 + eps) -> BF16, written 128B-swizzled into
-//                   shared memory as the next MMA's A operand
-//   MMA2  D2[128 x N]  += R[128 x 64] B2[N x 64]^T     (numerator, in TMEM)
-//   H-step: rows u; A1 = Hc (H, column-major BF16), B1 = Wr (W, row-major),
-//           V tile from Vb, B2 = Wb;                 K = i (rows of V)
-//   W-step: rows i; A1 = Wr, B1 = Hc, V tile from Vbt, B2 = Hb;  K = u
-// MMA1 of block g+1 is issued before MMA2 of block g so the tensor core
-// works while the epilogue warps form R.  Stream-K partition and partial
-// slots as in the Euclidean GEMM; the epilogue warps also finish the
-// column/row sums (the KL denominators) from the update kernel's partials.
+// never materialising W H.  Per 128-row output tile and 128-wide K block:
+//   MMA1  D1[128 x 128] = A1[128 x r] F[128 x r]^T     (S for the block, in TMEM)
+//   epilogue warps: R = V / (D1 + eps) -> BF16, stored back into the same
+//                   TMEM columns (two values per 32-bit column)
+//   MMA2  D2[128 x r]  += R[128 x 128] F[128 x r]      (numerator, in TMEM;
+//                   A read from TMEM, B = the same F tile read MN-major)
+//   H-step: rows u; A1 = Hc (H, column-major BF16), F = Wr (W, row-major),
+//           V tile from Vb;                  K = i (rows of V)
+//   W-step: rows i; A1 = Wr, F = Hc, V tile from Vbt;  K = u
+// One F tile serves both products, so a block moves 32 KB of V (HBM) and
+// r*256 bytes of F (L2) into shared memory, and the tensor pipe gets 8 + 8
+// instructions of N = 128 per block (r = 128), few enough for one issuing
+// thread.  V and F have separate rings: a V stage is released as soon as the
+// epilogue has read it, an F stage when MMA2 of its block completes.  TMEM
+// holds nb S/R buffers of 128 columns and the numerator accumulator, so MMA1
+// runs up to nb blocks ahead of the epilogue; the MMA thread polls its
+// barriers and issues whichever product is ready (MMA2 first, which frees
+// buffers).  Stream-K partition and partial slots as in the Euclidean GEMM;
+// the epilogue warps also finish the column/row sums (the KL denominators)
+// from the update kernel's partials.
 // ========================================================================
 struct KlParams {
-    int tiles, kblocks, npad, stages, max_seg, nbox;
-    uint32_t tmem_cols;
+    int tiles, kblocks, npad, max_seg, nbox;
+    int sv, sf, nb;  // V ring stages, F ring stages, S/R buffers in TMEM
     float eps;
     float *partials;
     int *err;
@@ -1236,287 +1244,341 @@ struct KlParams {
     int sum_count;
 };
 
+constexpr int kKlBlockK = 128;            // K columns per block
+constexpr int kKlVBytes = kTileM * kKlBlockK * 2;  // 32 KB: two 64-column boxes
+constexpr int kKlFBox = kKlBlockK * 128;  // 16 KB: 128 K-rows x 64 columns of the factor
+constexpr int kKlMaxSV = 6, kKlMaxSF = 8, kKlMaxNB = 3;
+constexpr int kKlBarBytes = 1024;  // barriers, the TMEM address, the denominator scratch
+
 __device__ __forceinline__ uint32_t sw128(int row, int chunk) {
     return (uint32_t)(row * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
-constexpr int kKlEpiWarps = 16;  // two groups of 8 (even / odd K blocks); 2 per TMEM lane quarter in a group
+__device__ __forceinline__ void ring_next(int &i, uint32_t &ph, int n) {
+    if (++i == n) {
+        i = 0;
+        ph ^= 1;
+    }
+}
+
+constexpr int kKlEpiWarps = 16;  // two groups of 8 (even / odd blocks); 2 per TMEM lane quarter in a group
 constexpr int kKlThreads = 64 + 32 * kKlEpiWarps;  // warp 0 TMA, warp 1 MMA, then the ratio epilogue
 
-__global__ void __launch_bounds__(kKlThreads, 1)
+// NK = npad / 16: the K16 steps of MMA1 (compile-time, so the MMA thread issues straight-line code)
+template <int NK>
+__global__ void __launch_bounds__(kKlThreads)
     tc_kl_gemm_kernel(const __grid_constant__ CUtensorMap tmV, const __grid_constant__ CUtensorMap tmA1,
-                      const __grid_constant__ CUtensorMap tmB1, const __grid_constant__ CUtensorMap tmB2,
-                      KlParams p) {
+                      const __grid_constant__ CUtensorMap tmF, KlParams p) {
+    constexpr int NP = NK * 16;
     const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
-    const int b1Bytes = p.nbox * 8192, b2Bytes = p.npad * 128;
-    const int stageBytes = 16384 + b1Bytes + b2Bytes;
-    unsigned char *sStage = reinterpret_cast<unsigned char *>(base);
-    unsigned char *sA1 = sStage + p.stages * stageBytes;
-    unsigned char *sR = sA1 + p.nbox * 16384;  // [2][16 KB]
-    uint64_t *full = reinterpret_cast<uint64_t *>(sR + 2 * 16384);
-    uint64_t *empty = full + p.stages;
-    uint64_t *a1full = empty + p.stages, *a1empty = a1full + 1;
-    uint64_t *d1full = a1empty + 1, *d1empty = d1full + 2;
-    uint64_t *rfull = d1empty + 2, *rempty = rfull + 2;
-    uint64_t *tfull = rempty + 2, *tempty = tfull + 2;
-    uint64_t *mdone = tempty + 2;
+    const int fBytes = p.nbox * kKlFBox;
+    unsigned char *sA1 = reinterpret_cast<unsigned char *>(base);
+    unsigned char *sFr = sA1 + p.nbox * 16384;
+    unsigned char *sVr = sFr + p.sf * fBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sVr + p.sv * kKlVBytes);
+    uint64_t *vfull = bars, *vempty = vfull + kKlMaxSV;
+    uint64_t *ffull = vempty + kKlMaxSV, *fempty = ffull + kKlMaxSF;
+    uint64_t *d1full = fempty + kKlMaxSF, *d1empty = d1full + kKlMaxNB, *rfull = d1empty + kKlMaxNB;
+    uint64_t *a1full = rfull + kKlMaxNB, *a1empty = a1full + 1;
+    uint64_t *tfull = a1empty + 1, *tempty = tfull + 1;
+    uint64_t *mdone = tempty + 1;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+    float *red = reinterpret_cast<float *>(mdone + 2);  // [16] per-warp sums of the denominators
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long T = (long long)p.tiles * p.kblocks;
     const long long lo = (long long)blockIdx.x * T / gridDim.x;
     const long long hi = (long long)(blockIdx.x + 1) * T / gridDim.x;
-    auto sV = [&](int st) { return sStage + st * stageBytes; };
-    auto sB1 = [&](int st) { return sStage + st * stageBytes + 16384; };
-    auto sB2 = [&](int st) { return sStage + st * stageBytes + 16384 + b1Bytes; };
+    auto sF = [&](int st) { return sFr + st * fBytes; };
+    auto sV = [&](int st) { return sVr + st * kKlVBytes; };
+    auto seg_end = [&](long long b) { return min(hi, (b / p.kblocks + 1) * p.kblocks); };
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < p.stages; s++) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+        for (int s = 0; s < p.sv; s++) {
+            mbar_init(&vfull[s], 1);
+            mbar_init(&vempty[s], kKlEpiWarps / 2);  // the 8 warps of the block's group
+        }
+        for (int s = 0; s < p.sf; s++) {
+            mbar_init(&ffull[s], 1);
+            mbar_init(&fempty[s], 1);
+        }
+        for (int b = 0; b < p.nb; b++) {
+            mbar_init(&d1full[b], 1);
+            mbar_init(&d1empty[b], 1);
+            mbar_init(&rfull[b], kKlEpiWarps / 2);
         }
         mbar_init(a1full, 1);
         mbar_init(a1empty, 1);
-        for (int b = 0; b < 2; b++) {
-            mbar_init(&d1full[b], 1);
-            mbar_init(&d1empty[b], kKlEpiWarps / 2);  // buffer b is handled by group b
-            mbar_init(&rfull[b], kKlEpiWarps / 2);
-            mbar_init(&rempty[b], 1);
-            mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], kKlEpiWarps);
-        }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, kKlEpiWarps);
         mbar_init(mdone, 1);
         fence_mbar_init();
         tma_prefetch_desc(&tmV);
         tma_prefetch_desc(&tmA1);
-        tma_prefetch_desc(&tmB1);
-        tma_prefetch_desc(&tmB2);
+        tma_prefetch_desc(&tmF);
     }
     if (warp == 0) {
-        tmem_alloc(tmem_slot, p.tmem_cols);
+        tmem_alloc(tmem_slot, 512);
         tmem_relinquish();
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t tD1 = tmem, tD2 = tmem + 128;  // D1: 2 x 64 columns, D2: 2 x npad columns
+    // TMEM columns: the numerator accumulator [0, npad), then nb S/R buffers of 128
+    const uint32_t tD2 = tmem, tD1 = tmem + (uint32_t)NP;
     griddep_wait();
     griddep_launch_dependents();
 
     if (warp == 0) {
         if (lane == 0) {
-            int stage = 0, seg = 0;
-            uint32_t phase = 0;
-            for (long long b = lo; b < hi;) {
+            int vi = 0, fi = 0, seg = 0;
+            uint32_t vph = 0, fph = 0;
+            // the last phase armed on each full barrier (bit set) and its parity, for the drain below
+            uint32_t armed_v = 0, par_v = 0, armed_f = 0, par_f = 0;
+            bool ok = true;
+            for (long long b = lo; b < hi && ok;) {
                 const int t = (int)(b / p.kblocks);
-                const long long e = min(hi, (long long)(t + 1) * p.kblocks);
+                const long long e = seg_end(b);
                 // the factor tile of this row tile (MMA1's A), once per segment
-                if (!mbar_wait(a1empty, (uint32_t)((seg & 1) ^ 1), p.err, kErrWaitEmpty)) break;
+                if (!mbar_wait_sleep(a1empty, (uint32_t)((seg & 1) ^ 1), p.err, kErrWaitEmpty)) break;
                 mbar_arrive_expect_tx(a1full, (uint32_t)(p.nbox * 16384));
                 for (int q = 0; q < p.nbox; q++) tma_load_2d(sA1 + q * 16384, &tmA1, q * 64, t * kTileM, a1full);
-                bool ok = true;
                 for (long long bb = b; bb < e; bb++) {
-                    const int kb = (int)(bb % p.kblocks);
-                    if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty)) {
+                    const int k0 = (int)(bb % p.kblocks) * kKlBlockK;
+                    if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty)) {
                         ok = false;
                         break;
                     }
-                    mbar_arrive_expect_tx(&full[stage], (uint32_t)stageBytes);
-                    tma_load_2d(sV(stage), &tmV, kb * kBlockK, t * kTileM, &full[stage]);
-                    for (int q = 0; q < p.nbox; q++)
-                        tma_load_2d(sB1(stage) + q * 8192, &tmB1, q * 64, kb * kBlockK, &full[stage]);
-                    tma_load_2d(sB2(stage), &tmB2, kb * kBlockK, 0, &full[stage]);
-                    if (++stage == p.stages) {
-                        stage = 0;
-                        phase ^= 1;
+                    mbar_arrive_expect_tx(&ffull[fi], (uint32_t)fBytes);
+                    for (int q = 0; q < p.nbox; q++) tma_load_2d(sF(fi) + q * kKlFBox, &tmF, q * 64, k0, &ffull[fi]);
+                    armed_f |= 1u << fi;
+                    par_f = (par_f & ~(1u << fi)) | (fph << fi);
+                    ring_next(fi, fph, p.sf);
+                    if (!mbar_wait_sleep(&vempty[vi], vph ^ 1, p.err, kErrWaitEmpty)) {
+                        ok = false;
+                        break;
                     }
+                    mbar_arrive_expect_tx(&vfull[vi], (uint32_t)kKlVBytes);
+                    tma_load_2d(sV(vi), &tmV, k0, t * kTileM, &vfull[vi]);
+                    tma_load_2d(sV(vi) + kKlVBytes / 2, &tmV, k0 + 64, t * kTileM, &vfull[vi]);
+                    armed_v |= 1u << vi;
+                    par_v = (par_v & ~(1u << vi)) | (vph << vi);
+                    ring_next(vi, vph, p.sv);
                 }
-                if (!ok) break;
                 seg++;
                 b = e;
             }
+            // no copy of this CTA may still be landing when it exits (after an error the consumers
+            // stop early): wait, bounded, for the last phase armed on every barrier
+            for (int s = 0; s < p.sf; s++)
+                if (armed_f >> s & 1) mbar_wait_quiet(&ffull[s], par_f >> s & 1);
+            for (int s = 0; s < p.sv; s++)
+                if (armed_v >> s & 1) mbar_wait_quiet(&vfull[s], par_v >> s & 1);
+            if (seg > 0) mbar_wait_quiet(a1full, (uint32_t)((seg - 1) & 1));
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t id1 = idesc_bf16_f32(kTileM, 64), id2 = idesc_bf16_f32(kTileM, p.npad);
-            int stage = 0, seg = 0;
-            uint32_t phase = 0;
-            long long g = 0;  // global block counter (D1 / R double buffers)
-            bool ok = true;
-            int prev_stage = 0;
-            for (long long b = lo; b < hi && ok;) {
-                const int t = (int)(b / p.kblocks);
-                const long long e = min(hi, (long long)(t + 1) * p.kblocks);
-                const int acc = seg & 1;
-                if (!mbar_wait(a1full, (uint32_t)(seg & 1), p.err, kErrWaitFull)) break;
-                if (!mbar_wait(&tempty[acc], (uint32_t)(((seg >> 1) & 1) ^ 1), p.err, kErrWaitTmemEmpty)) break;
-                tc_fence_after();
-                const uint32_t a1 = smem_u32(sA1);
-                bool first2 = true;
-                for (long long bb = b; bb <= e && ok; bb++) {
-                    if (bb < e) {
-                        // MMA1 for block g
-                        const int db = (int)(g & 1);
-                        if (!mbar_wait(&full[stage], phase, p.err, kErrWaitFull) ||
-                            !mbar_wait(&d1empty[db], (uint32_t)(((g >> 1) & 1) ^ 1), p.err, kErrWaitTmemEmpty)) {
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint32_t b1 = smem_u32(sB1(stage));
-                        for (int k16 = 0; k16 < p.npad / 16; k16++) {
-                            const int q = k16 >> 2, w = (k16 & 3) * 32;
-                            tc_mma_f16(tD1 + (uint32_t)(db * 64), smem_desc(a1 + q * 16384 + w, 16, 1024, 2),
-                                       smem_desc(b1 + q * 8192 + w, 16, 1024, 2), id1, k16 > 0 ? 1u : 0u);
-                        }
-                        tc_commit(&d1full[db]);
-                    }
-                    if (bb > b) {
-                        // MMA2 for block g-1 (its R is formed by the epilogue warps)
-                        const long long gp = g - 1;
-                        const int rb = (int)(gp & 1);
-                        if (!mbar_wait(&rfull[rb], (uint32_t)((gp >> 1) & 1), p.err, kErrWaitFull)) {
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint32_t ra = smem_u32(sR + rb * 16384), b2 = smem_u32(sB2(prev_stage));
+            const uint32_t id1 = idesc_bf16_f32(kTileM, kKlBlockK);
+            const uint32_t id2 = idesc_bf16_f32(kTileM, NP) | kIdescBMnMajor;
+            // descriptors of A1 and of F stage 0 (K-major for MMA1, MN-major for MMA2: the factor's
+            // 64-column boxes are the MN chunks, 16 KB apart); a stage or a K step moves the start
+            // address, which is the descriptor's low bits (address >> 4)
+            const uint64_t a1d = smem_desc(smem_u32(sA1), 16, 1024, 2);
+            const uint64_t fdk = smem_desc(smem_u32(sFr), 16, 1024, 2);
+            const uint64_t fdm = smem_desc(smem_u32(sFr), kKlFBox, 1024, 2);
+            const uint32_t fstep = (uint32_t)fBytes >> 4;
+            // blocks of this CTA counted from 0; a segment ends at a tile boundary
+            const int nblk = (int)(hi - lo);
+            auto seg_end_local = [&](int j) { return (int)(seg_end(lo + j) - lo); };
+            // MMA1 cursor: block j1, its F stage and S/R buffer, its segment
+            int j1 = 0, e1 = seg_end_local(0), f1 = 0, d1 = 0, seg1 = 0;
+            uint32_t f1ph = 0, d1ph = 0;
+            bool a1_ready = false;
+            // MMA2 cursor
+            int j2 = 0, e2 = e1, f2 = 0, d2 = 0, seg2 = 0;
+            uint32_t f2ph = 0, d2ph = 0;
+            bool first2 = true;
+            long long t_idle = 0;
+            int spins = 0;
+            while (j2 < nblk) {
+                bool did = false;
+                // MMA2 of the oldest block whose R is in TMEM (frees its F stage and S/R buffer)
+                if (j2 < j1 && mbar_test(&rfull[d2], d2ph)) {
+                    // the accumulator of a new segment: the previous segment's numerator drained
+                    if (first2 && seg2 > 0 && !mbar_wait(tempty, (uint32_t)((seg2 - 1) & 1), p.err, kErrWaitTmemEmpty))
+                        break;
+                    tc_fence_after();
+                    const uint64_t fb = fdm + (uint64_t)(f2 * fstep);
+                    const uint32_t rb = tD1 + (uint32_t)(d2 * kKlBlockK);
 #pragma unroll
-                        for (int k = 0; k < 4; k++)
-                            tc_mma_f16(tD2 + (uint32_t)(acc * p.npad), smem_desc(ra + k * 32, 16, 1024, 2),
-                                       smem_desc(b2 + k * 32, 16, 1024, 2), id2, (first2 && k == 0) ? 0u : 1u);
-                        first2 = false;
-                        tc_commit(&empty[prev_stage]);
-                        tc_commit(&rempty[rb]);
+                    for (int k = 0; k < kKlBlockK / 16; k++)  // R of part p at columns 64p .. 64p + 31
+                        tc_mma_f16_ts(tD2, rb + (uint32_t)((k >> 2) * 64 + (k & 3) * 8), fb + (uint64_t)(k * 2048 >> 4),
+                                      id2, (first2 && k == 0) ? 0u : 1u);
+                    tc_commit(&fempty[f2]);
+                    tc_commit(&d1empty[d2]);
+                    first2 = false;
+                    ring_next(f2, f2ph, p.sf);
+                    ring_next(d2, d2ph, p.nb);
+                    if (++j2 == e2) {
+                        tc_commit(tfull);
+                        seg2++;
+                        first2 = true;
+                        if (j2 < nblk) e2 = seg_end_local(j2);
                     }
-                    if (bb < e) {
-                        prev_stage = stage;
-                        if (++stage == p.stages) {
-                            stage = 0;
-                            phase ^= 1;
+                    did = true;
+                }
+                // MMA1 of the next block once its F tile, a free S/R buffer and its A1 are there
+                if (j1 < nblk) {
+                    if (!a1_ready) a1_ready = mbar_test(a1full, (uint32_t)(seg1 & 1));
+                    if (a1_ready && mbar_test(&ffull[f1], f1ph) && mbar_test(&d1empty[d1], d1ph ^ 1)) {
+                        tc_fence_after();
+                        const uint64_t fb = fdk + (uint64_t)(f1 * fstep);
+                        const uint32_t dd = tD1 + (uint32_t)(d1 * kKlBlockK);
+#pragma unroll
+                        for (int k16 = 0; k16 < NK; k16++) {
+                            const int off = (k16 >> 2) * 16384 + (k16 & 3) * 32, offf = (k16 >> 2) * kKlFBox + (k16 & 3) * 32;
+                            tc_mma_f16(dd, a1d + (uint64_t)(off >> 4), fb + (uint64_t)(offf >> 4), id1, k16 > 0 ? 1u : 0u);
                         }
-                        g++;
+                        tc_commit(&d1full[d1]);
+                        ring_next(f1, f1ph, p.sf);
+                        ring_next(d1, d1ph, p.nb);
+                        if (++j1 == e1) {
+                            tc_commit(a1empty);  // A1 free once this segment's products are done
+                            seg1++;
+                            a1_ready = false;
+                            if (j1 < nblk) e1 = seg_end_local(j1);
+                        }
+                        did = true;
                     }
                 }
-                if (!ok) break;
-                tc_commit(&tfull[acc]);
-                tc_commit(a1empty);
-                seg++;
-                b = e;
+                if (did) {
+                    spins = 0;
+                    t_idle = 0;
+                } else if (++spins == 256) {  // idle: check the error word and the time limit now and then
+                    spins = 0;
+                    if (*((volatile int *)p.err) != 0) break;
+                    const long long now = clock64();
+                    if (t_idle == 0) {
+                        t_idle = now;
+                    } else if (now - t_idle > kWaitLimitCycles) {
+                        atomicOr(p.err, kErrWaitFull);
+                        break;
+                    }
+                }
             }
             tc_commit(mdone);
             mbar_wait_quiet(mdone, 0);
         }
     } else {
-        // finish the denominators (column / row sums of the other factor) from the partials
+        // finish the denominators (column / row sums of the other factor) from the partials: each of
+        // this CTA's entries by all 512 epilogue threads (thread et takes partials et, et + 512, ...,
+        // then a fixed tree over lanes and warps), so no warp starts the ratios much later than the rest
         if (p.sum_out) {
-            const int et = threadIdx.x - 64;  // 0 .. 255
+            const int et = threadIdx.x - 64;  // 0 .. 511
             const int E = p.npad;
             const int e0 = (int)((long long)blockIdx.x * E / gridDim.x), e1 = (int)((long long)(blockIdx.x + 1) * E / gridDim.x);
-            for (int eb = e0; eb < e1; eb += kKlEpiWarps * 8) {
-                const int ei = eb + (et >> 2);
-                float sacc = 0.f;
-                if (ei < e1) {
-                    int z = et & 3;
-                    for (; z + 28 < p.sum_count; z += 32) {
-                        float v[8];
+            for (int ei = e0; ei < e1; ei++) {
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                int z = et;
+                for (; z + 3 * 512 < p.sum_count; z += 4 * 512) {
 #pragma unroll
-                        for (int q = 0; q < 8; q++) v[q] = p.sum_partials[(size_t)(z + 4 * q) * E + ei];
-#pragma unroll
-                        for (int q = 0; q < 8; q++) sacc += v[q];
-                    }
-                    for (; z < p.sum_count; z += 4) sacc += p.sum_partials[(size_t)z * E + ei];
+                    for (int q = 0; q < 4; q++) v[q] += p.sum_partials[(size_t)(z + q * 512) * E + ei];
                 }
-                sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
-                sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
-                if (ei < e1 && (et & 3) == 0) p.sum_out[ei] = sacc;
+#pragma unroll
+                for (int q = 0; q < 3; q++)  // at most three left
+                    if (z + q * 512 < p.sum_count) v[q] += p.sum_partials[(size_t)(z + q * 512) * E + ei];
+                float sacc = (v[0] + v[1]) + (v[2] + v[3]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+                if (lane == 0) red[warp - 2] = sacc;
+                asm volatile("bar.sync 3, 512;" ::: "memory");
+                if (et == 0) {
+                    float t = 0.f;
+                    for (int w = 0; w < kKlEpiWarps; w++) t += red[w];
+                    p.sum_out[ei] = t;
+                }
+                asm volatile("bar.sync 3, 512;" ::: "memory");
             }
         }
         const int quarter = warp & 3;           // TMEM lanes this warp may access
-        const int grp = (warp - 2) >> 3;         // group 0 takes even K blocks, group 1 odd ones
-        const int part = ((warp - 2) >> 2) & 1;  // which 32 of the block's 64 columns
+        const int grp = (warp - 2) >> 3;         // group 0 takes even blocks, group 1 odd ones
+        const int part = ((warp - 2) >> 2) & 1;  // which 64 of the block's 128 columns (= V box)
         const int dpart = (warp - 2) >> 2;       // 0..3: share of the D2 drain
         const float eps_pos = fmaxf(p.eps, 1e-30f);
         const int row = quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
-        int stage = 0, seg = 0;
-        uint32_t sphase = 0;
+        int vi = 0, di = 0, seg = 0;
+        uint32_t vph = 0, dph = 0;
         long long g = 0;
         for (long long b = lo; b < hi;) {
-            const int t = (int)(b / p.kblocks);
-            const long long e = min(hi, (long long)(t + 1) * p.kblocks);
+            const long long e = seg_end(b);
             bool ok = true;
-            for (long long bb = b; bb < e; bb++) {
-                const int db = (int)(g & 1);
-                if (db != grp) {  // the other group's block: keep the counters in step
-                    if (++stage == p.stages) {
-                        stage = 0;
-                        sphase ^= 1;
-                    }
-                    g++;
+            for (long long bb = b; bb < e; bb++, g++) {
+                if ((int)(g & 1) != grp) {  // the other group's block: keep the cursors in step
+                    ring_next(vi, vph, p.sv);
+                    ring_next(di, dph, p.nb);
                     continue;
                 }
-                if (!warp_wait(&d1full[db], (uint32_t)((g >> 1) & 1), p.err, kErrWaitTmemFull) ||
-                    !warp_wait(&full[stage], sphase, p.err, kErrWaitFull) ||
-                    !warp_wait(&rempty[db], (uint32_t)(((g >> 1) & 1) ^ 1), p.err, kErrWaitEmpty)) {
+                if (!mbar_wait_sleep(&d1full[di], dph, p.err, kErrWaitTmemFull) ||
+                    !mbar_wait_sleep(&vfull[vi], vph, p.err, kErrWaitFull)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const unsigned char *vt = sV(stage);
-                unsigned char *rt = sR + db * 16384;
-                // this warp's 32 columns of S for its row: two loads in flight, one wait
-                float sv[32];
-                {
-                    float (&s0)[16] = *reinterpret_cast<float (*)[16]>(&sv[0]);
-                    float (&s1)[16] = *reinterpret_cast<float (*)[16]>(&sv[16]);
-                    const uint32_t ta = tD1 + (uint32_t)(db * 64 + part * 32) + lane_off;
-                    tmem_ld16(ta, s0);
-                    tmem_ld16(ta + 16, s1);
-                    tmem_ld_wait();
-                }
+                const unsigned char *vt = sV(vi) + part * (kKlVBytes / 2);  // this part's 64-column box
+                const uint32_t tb = tD1 + (uint32_t)(di * kKlBlockK + part * 64) + lane_off;
 #pragma unroll
-                for (int cc = 0; cc < 4; cc++) {  // 16-byte chunks of 8 values
-                    const int chunk = part * 4 + cc;
-                    const uint4 vraw = *reinterpret_cast<const uint4 *>(vt + sw128(row, chunk));
-                    const __nv_bfloat162 *v2 = reinterpret_cast<const __nv_bfloat162 *>(&vraw);
-                    uint4 out;
-                    __nv_bfloat162 *o2 = reinterpret_cast<__nv_bfloat162 *>(&out);
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        // R is rounded to BF16 (8-bit significand): the approximate division
-                        // (2 ulp in FP32) is exact enough.  eps_pos > 0 keeps zero-padded
-                        // entries (V = 0, S = 0) at 0.
-                        const float2 vf = __bfloat1622float2(v2[q]);
-                        const float r0 = __fdividef(vf.x, sv[cc * 8 + 2 * q] + eps_pos);
-                        const float r1 = __fdividef(vf.y, sv[cc * 8 + 2 * q + 1] + eps_pos);
-                        o2[q] = __floats2bfloat162_rn(r0, r1);
+                for (int h = 0; h < 2; h++) {  // 32 of this warp's 64 columns at a time
+                    float sv[32];
+                    {
+                        float (&s0)[16] = *reinterpret_cast<float (*)[16]>(&sv[0]);
+                        float (&s1)[16] = *reinterpret_cast<float (*)[16]>(&sv[16]);
+                        tmem_ld16(tb + (uint32_t)(h * 32), s0);
+                        tmem_ld16(tb + (uint32_t)(h * 32 + 16), s1);
                     }
-                    *reinterpret_cast<uint4 *>(rt + sw128(row, chunk)) = out;
+                    uint4 vraw[4];
+#pragma unroll
+                    for (int cc = 0; cc < 4; cc++) vraw[cc] = *reinterpret_cast<const uint4 *>(vt + sw128(row, h * 4 + cc));
+                    if (h == 1) {  // the V stage is read (the arrive orders the loads before the refill)
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&vempty[vi]);
+                    }
+                    tmem_ld_wait();
+                    uint32_t rr[16];
+#pragma unroll
+                    for (int cc = 0; cc < 4; cc++) {
+                        const __nv_bfloat162 *v2 = reinterpret_cast<const __nv_bfloat162 *>(&vraw[cc]);
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            // R is rounded to BF16 (8-bit significand): the approximate division
+                            // (2 ulp in FP32) is exact enough.  eps_pos > 0 keeps zero-padded
+                            // entries (V = 0, S = 0) at 0.
+                            const float2 vf = __bfloat1622float2(v2[q]);
+                            const float r0 = __fdividef(vf.x, sv[cc * 8 + 2 * q] + eps_pos);
+                            const float r1 = __fdividef(vf.y, sv[cc * 8 + 2 * q + 1] + eps_pos);
+                            const __nv_bfloat162 o = __floats2bfloat162_rn(r0, r1);
+                            rr[cc * 4 + q] = *reinterpret_cast<const uint32_t *>(&o);
+                        }
+                    }
+                    // R (packed pairs) over S columns this warp has already read: half h of the
+                    // part's R goes to its columns 16h .. 16h + 15
+                    tmem_st16(tb + (uint32_t)(h * 16), rr);
                 }
-                // R written with ordinary stores: make it visible to the tensor core, then hand it over
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                tmem_st_wait();
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) {
-                    mbar_arrive(&rfull[db]);
-                    mbar_arrive(&d1empty[db]);
-                }
-                if (++stage == p.stages) {
-                    stage = 0;
-                    sphase ^= 1;
-                }
-                g++;
+                if (lane == 0) mbar_arrive(&rfull[di]);
+                ring_next(vi, vph, p.sv);
+                ring_next(di, dph, p.nb);
             }
             if (!ok) break;
-            const int acc = seg & 1;
-            if (!warp_wait(&tfull[acc], (uint32_t)((seg >> 1) & 1), p.err, kErrWaitTmemFull)) break;
+            if (!mbar_wait_sleep(tfull, (uint32_t)(seg & 1), p.err, kErrWaitTmemFull)) break;
             tc_fence_after();
             float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
-            for (int c = dpart * 16; c < p.npad; c += 64) {  // the four warps of a quarter take turns by 16 columns
+            for (int c = dpart * 16; c < NP; c += 64) {  // the four warps of a quarter take turns by 16 columns
                 float v[16];
-                tmem_ld16(tD2 + (uint32_t)(acc * p.npad) + lane_off + (uint32_t)c, v);
+                tmem_ld16(tD2 + lane_off + (uint32_t)c, v);
                 tmem_ld_wait();
                 float4 *d4 = reinterpret_cast<float4 *>(dst + c);
                 d4[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -1526,7 +1588,7 @@ __global__ void __launch_bounds__(kKlThreads, 1)
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[acc]);
+            if (lane == 0) mbar_arrive(tempty);
             seg++;
             b = e;
         }
@@ -1534,7 +1596,7 @@ __global__ void __launch_bounds__(kKlThreads, 1)
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tmem, p.tmem_cols);
+        tmem_dealloc(tmem, 512);
     }
 }
 
@@ -1680,7 +1742,7 @@ struct TcGemm {
 };
 
 struct KlGemm {
-    CUtensorMap tmV, tmA1, tmB1, tmB2;
+    CUtensorMap tmV, tmA1, tmF;
     gpunmf::KlParams p;
     int grid = 0, smem = 0;
     int *slot_ptr = nullptr, *slot_list = nullptr, *tile_slots = nullptr;
@@ -2010,7 +2072,6 @@ static UpdParams update_params_w(gpunmf_job *j, int update) {
     return u;
 }
 
-constexpr int kKlSmemBudget = 220 * 1024;
 constexpr int kKlMaxRank = 128;
 
 static cudaError_t set_kl_smem_once() {
@@ -2020,15 +2081,18 @@ static cudaError_t set_kl_smem_once() {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         result = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (result == cudaSuccess)
-            result = cudaFuncSetAttribute(tc_kl_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+#define KLATTR(NK)                                                                                     \
+    if (result == cudaSuccess)                                                                         \
+        result = cudaFuncSetAttribute(tc_kl_gemm_kernel<NK>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        KLATTR(1) KLATTR(2) KLATTR(3) KLATTR(4) KLATTR(5) KLATTR(6) KLATTR(7) KLATTR(8)
+#undef KLATTR
     });
     return result;
 }
 
 static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npad, float **partials, int *err) {
     const int tiles = ceil_div(rows, kTileM);
-    const int kblocks = ceil_div(K, kBlockK);
+    const int kblocks = ceil_div(K, kKlBlockK);
     const long long T = (long long)tiles * kblocks;
     g.grid = (int)std::min<long long>(num_sms(), T);
     std::vector<int> ptr, list;
@@ -2043,24 +2107,30 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
         for (int t = 0; t < tiles; t++)
             for (int q = ptr[t]; q < ptr[t + 1]; q++) table[(size_t)t * kSlotW + (q - ptr[t])] = list[q];
     }
+    // shared memory: A1 (nbox 16 KB boxes), the F ring (nbox 16 KB boxes a stage), the V ring
+    // (32 KB a stage), barriers.  V stages are split evenly with F's bytes; an F stage is held
+    // longer (until MMA2 of its block completes), so F gets the remainder.
     const int nbox = (npad + 63) / 64;
-    const int stage_bytes = 16384 + nbox * 8192 + npad * 128;
-    const int fixed = 1024 + nbox * 16384 + 2 * 16384 + 512;
-    const int stages = std::min(kMaxStages, (kKlSmemBudget - fixed) / stage_bytes);
-    if (stages < 2) {
+    const int fbytes = nbox * kKlFBox;
+    const int fixed = 1024 + nbox * 16384 + kKlBarBytes;
+    const int room = smem_optin() - fixed;
+    const int sv = std::max(2, std::min(kKlMaxSV, room / 2 / kKlVBytes));
+    const int sf = std::min(kKlMaxSF, (room - sv * kKlVBytes) / fbytes);
+    if (sf < 2 || fixed + sv * kKlVBytes + sf * fbytes > smem_optin()) {
         set_error("KL tensor-core kernel: rank too large for the shared-memory pipeline");
         return GPUNMF_ERR_UNSUPPORTED;
     }
     g.p.tiles = tiles;
     g.p.kblocks = kblocks;
     g.p.npad = npad;
-    g.p.stages = stages;
     g.p.max_seg = max_seg;
     g.p.nbox = nbox;
-    g.p.tmem_cols = (128 + 2 * npad) <= 256 ? 256 : 512;
+    g.p.sv = sv;
+    g.p.sf = sf;
+    g.p.nb = std::min(kKlMaxNB, (512 - npad) / kKlBlockK);  // S/R buffers beside the accumulator
     g.p.eps = j->eps;
     g.p.err = err;
-    g.smem = fixed + stages * stage_bytes;
+    g.smem = fixed + sv * kKlVBytes + sf * fbytes;
     size_t slots = (size_t)g.grid * max_seg;
     cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.slot_ptr, ptr.size() * sizeof(int));
@@ -2091,7 +2161,13 @@ static cudaError_t launch_kl_gemm(KlGemm &g, cudaStream_t s) {
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, tc_kl_gemm_kernel, g.tmV, g.tmA1, g.tmB1, g.tmB2, g.p);
+    switch (g.p.npad / 16) {
+#define KLCASE(NK) \
+    case NK: return cudaLaunchKernelEx(&cfg, tc_kl_gemm_kernel<NK>, g.tmV, g.tmA1, g.tmF, g.p);
+        KLCASE(1) KLCASE(2) KLCASE(3) KLCASE(4) KLCASE(5) KLCASE(6) KLCASE(7) KLCASE(8)
+#undef KLCASE
+    }
+    return cudaErrorInvalidValue;
 }
 
 static cudaError_t launch_kl_update(const KlUpdParams &u, int rp, bool is_w, cudaStream_t s) {
@@ -2169,16 +2245,14 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
     if (st != GPUNMF_OK) return st;
     t->kh.p.sum_partials = t->SP_w; t->kh.p.sum_out = t->S_w; t->kh.p.sum_count = cw;
     t->kw.p.sum_partials = t->SP_h; t->kw.p.sum_out = t->S_h; t->kw.p.sum_count = ch;
-    // H-step: rows u; V tile from Vb, A1 = Hc rows u, B1 = Wr rows i, B2 = Wb
+    // H-step: rows u; V tile from Vb, A1 = Hc rows u, F = Wr rows i
     st = make_map(&t->kh.tmV, t->Vb, n, m, t->ldv, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->kh.tmA1, t->Hc, r, m, t->ldr, kTileM);
-    if (st == GPUNMF_OK) st = make_map(&t->kh.tmB1, t->Wr, r, n, t->ldr, kBlockK);
-    if (st == GPUNMF_OK) st = make_map(&t->kh.tmB2, t->Wb, n, r, t->ldw, t->npad);
-    // W-step: rows i; V tile from Vbt, A1 = Wr rows i, B1 = Hc rows u, B2 = Hb
+    if (st == GPUNMF_OK) st = make_map(&t->kh.tmF, t->Wr, r, n, t->ldr, kKlBlockK);
+    // W-step: rows i; V tile from Vbt, A1 = Wr rows i, F = Hc rows u
     if (st == GPUNMF_OK) st = make_map(&t->kw.tmV, t->Vbt, m, n, t->ldvt, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->kw.tmA1, t->Wr, r, n, t->ldr, kTileM);
-    if (st == GPUNMF_OK) st = make_map(&t->kw.tmB1, t->Hc, r, m, t->ldr, kBlockK);
-    if (st == GPUNMF_OK) st = make_map(&t->kw.tmB2, t->Hb, m, r, t->ldh, t->npad);
+    if (st == GPUNMF_OK) st = make_map(&t->kw.tmF, t->Hc, r, m, t->ldr, kKlBlockK);
     if (st != GPUNMF_OK) return st;
     GPUNMF_CUDA_TRY(set_kl_smem_once());
     return setup_quality(j);
