@@ -1254,6 +1254,13 @@ __device__ __forceinline__ uint32_t sw128(int row, int chunk) {
     return (uint32_t)(row * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
+// one lane of the (fully active) warp, the same every call
+__device__ __forceinline__ bool elect_one() {
+    uint32_t pred = 0;
+    asm volatile("{\n\t.reg .pred P;\n\telect.sync _|P, 0xffffffff;\n\tselp.b32 %0, 1, 0, P;\n\t}" : "=r"(pred));
+    return pred != 0;
+}
+
 __device__ __forceinline__ void ring_next(int &i, uint32_t &ph, int n) {
     if (++i == n) {
         i = 0;
@@ -1261,7 +1268,7 @@ __device__ __forceinline__ void ring_next(int &i, uint32_t &ph, int n) {
     }
 }
 
-constexpr int kKlEpiWarps = 16;  // two groups of 8 (even / odd blocks); 2 per TMEM lane quarter in a group
+constexpr int kKlEpiWarps = 16;  // 4 per TMEM lane quarter, 32 columns of each block each
 constexpr int kKlThreads = 64 + 32 * kKlEpiWarps;  // warp 0 TMA, warp 1 MMA, then the ratio epilogue
 
 // NK = npad / 16: the K16 steps of MMA1 (compile-time, so the MMA thread issues straight-line code)
@@ -1296,7 +1303,7 @@ __global__ void __launch_bounds__(kKlThreads)
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.sv; s++) {
             mbar_init(&vfull[s], 1);
-            mbar_init(&vempty[s], kKlEpiWarps / 2);  // the 8 warps of the block's group
+            mbar_init(&vempty[s], kKlEpiWarps);  // every epilogue warp reads its part of each V tile
         }
         for (int s = 0; s < p.sf; s++) {
             mbar_init(&ffull[s], 1);
@@ -1305,7 +1312,7 @@ __global__ void __launch_bounds__(kKlThreads)
         for (int b = 0; b < p.nb; b++) {
             mbar_init(&d1full[b], 1);
             mbar_init(&d1empty[b], 1);
-            mbar_init(&rfull[b], kKlEpiWarps / 2);
+            mbar_init(&rfull[b], kKlEpiWarps);
         }
         mbar_init(a1full, 1);
         mbar_init(a1empty, 1);
@@ -1378,60 +1385,68 @@ __global__ void __launch_bounds__(kKlThreads)
             if (seg > 0) mbar_wait_quiet(a1full, (uint32_t)((seg - 1) & 1));
         }
     } else if (warp == 1) {
-        if (lane == 0) {
-            const uint32_t id1 = idesc_bf16_f32(kTileM, kKlBlockK);
-            const uint32_t id2 = idesc_bf16_f32(kTileM, NP) | kIdescBMnMajor;
-            // descriptors of A1 and of F stage 0 (K-major for MMA1, MN-major for MMA2: the factor's
-            // 64-column boxes are the MN chunks, 16 KB apart); a stage or a K step moves the start
-            // address, which is the descriptor's low bits (address >> 4)
-            const uint64_t a1d = smem_desc(smem_u32(sA1), 16, 1024, 2);
-            const uint64_t fdk = smem_desc(smem_u32(sFr), 16, 1024, 2);
-            const uint64_t fdm = smem_desc(smem_u32(sFr), kKlFBox, 1024, 2);
-            const uint32_t fstep = (uint32_t)fBytes >> 4;
-            // blocks of this CTA counted from 0; a segment ends at a tile boundary
-            const int nblk = (int)(hi - lo);
-            auto seg_end_local = [&](int j) { return (int)(seg_end(lo + j) - lo); };
-            // MMA1 cursor: block j1, its F stage and S/R buffer, its segment
-            int j1 = 0, e1 = seg_end_local(0), f1 = 0, d1 = 0, seg1 = 0;
-            uint32_t f1ph = 0, d1ph = 0;
-            bool a1_ready = false;
-            // MMA2 cursor
-            int j2 = 0, e2 = e1, f2 = 0, d2 = 0, seg2 = 0;
-            uint32_t f2ph = 0, d2ph = 0;
-            bool first2 = true;
-            long long t_idle = 0;
-            int spins = 0;
-            while (j2 < nblk) {
-                bool did = false;
-                // MMA2 of the oldest block whose R is in TMEM (frees its F stage and S/R buffer)
-                if (j2 < j1 && mbar_test(&rfull[d2], d2ph)) {
-                    // the accumulator of a new segment: the previous segment's numerator drained
-                    if (first2 && seg2 > 0 && !mbar_wait(tempty, (uint32_t)((seg2 - 1) & 1), p.err, kErrWaitTmemEmpty))
-                        break;
+        // The whole warp runs the MMA loop (its state is warp-uniform, barrier tests are voted), and
+        // one elected lane issues the products and commits: the issue path stays on warp-uniform
+        // values instead of a single divergent lane.
+        const uint32_t id1 = idesc_bf16_f32(kTileM, kKlBlockK);
+        const uint32_t id2 = idesc_bf16_f32(kTileM, NP) | kIdescBMnMajor;
+        // descriptors of A1 and of F stage 0 (K-major for MMA1, MN-major for MMA2: the factor's
+        // 64-column boxes are the MN chunks, 16 KB apart); a stage or a K step moves the start
+        // address, which is the descriptor's low bits (address >> 4)
+        const uint64_t a1d = smem_desc(smem_u32(sA1), 16, 1024, 2);
+        const uint64_t fdk = smem_desc(smem_u32(sFr), 16, 1024, 2);
+        const uint64_t fdm = smem_desc(smem_u32(sFr), kKlFBox, 1024, 2);
+        const uint32_t fstep = (uint32_t)fBytes >> 4;
+        const bool leader = elect_one();
+        // blocks of this CTA counted from 0; a segment ends at a tile boundary
+        const int nblk = (int)(hi - lo);
+        auto seg_end_local = [&](int j) { return (int)(seg_end(lo + j) - lo); };
+        // MMA1 cursor: block j1, its F stage and S/R buffer, its segment
+        int j1 = 0, e1 = seg_end_local(0), f1 = 0, d1 = 0, seg1 = 0;
+        uint32_t f1ph = 0, d1ph = 0;
+        bool a1_ready = false;
+        // MMA2 cursor
+        int j2 = 0, e2 = e1, f2 = 0, d2 = 0, seg2 = 0;
+        uint32_t f2ph = 0, d2ph = 0;
+        bool first2 = true;
+        long long t_idle = 0;
+        int spins = 0;
+        while (j2 < nblk) {
+            bool did = false;
+            // MMA2 of the oldest block whose R is in TMEM (frees its F stage and S/R buffer)
+            if (j2 < j1 && __all_sync(0xffffffffu, mbar_test(&rfull[d2], d2ph))) {
+                // the accumulator of a new segment: the previous segment's numerator drained
+                if (first2 && seg2 > 0 &&
+                    !__all_sync(0xffffffffu, mbar_wait(tempty, (uint32_t)((seg2 - 1) & 1), p.err, kErrWaitTmemEmpty)))
+                    break;
+                if (leader) {
                     tc_fence_after();
                     const uint64_t fb = fdm + (uint64_t)(f2 * fstep);
                     const uint32_t rb = tD1 + (uint32_t)(d2 * kKlBlockK);
 #pragma unroll
-                    for (int k = 0; k < kKlBlockK / 16; k++)  // R of part p at columns 64p .. 64p + 31
-                        tc_mma_f16_ts(tD2, rb + (uint32_t)((k >> 2) * 64 + (k & 3) * 8), fb + (uint64_t)(k * 2048 >> 4),
+                    for (int k = 0; k < kKlBlockK / 16; k++)  // R of part p at columns 32p .. 32p + 15
+                        tc_mma_f16_ts(tD2, rb + (uint32_t)((k >> 1) * 32 + (k & 1) * 8), fb + (uint64_t)(k * 2048 >> 4),
                                       id2, (first2 && k == 0) ? 0u : 1u);
                     tc_commit(&fempty[f2]);
                     tc_commit(&d1empty[d2]);
-                    first2 = false;
-                    ring_next(f2, f2ph, p.sf);
-                    ring_next(d2, d2ph, p.nb);
-                    if (++j2 == e2) {
-                        tc_commit(tfull);
-                        seg2++;
-                        first2 = true;
-                        if (j2 < nblk) e2 = seg_end_local(j2);
-                    }
-                    did = true;
+                    if (j2 + 1 == e2) tc_commit(tfull);
                 }
-                // MMA1 of the next block once its F tile, a free S/R buffer and its A1 are there
-                if (j1 < nblk) {
-                    if (!a1_ready) a1_ready = mbar_test(a1full, (uint32_t)(seg1 & 1));
-                    if (a1_ready && mbar_test(&ffull[f1], f1ph) && mbar_test(&d1empty[d1], d1ph ^ 1)) {
+                __syncwarp();
+                first2 = false;
+                ring_next(f2, f2ph, p.sf);
+                ring_next(d2, d2ph, p.nb);
+                if (++j2 == e2) {
+                    seg2++;
+                    first2 = true;
+                    if (j2 < nblk) e2 = seg_end_local(j2);
+                }
+                did = true;
+            }
+            // MMA1 of the next block once its F tile, a free S/R buffer and its A1 are there
+            if (j1 < nblk) {
+                if (!a1_ready) a1_ready = __all_sync(0xffffffffu, mbar_test(a1full, (uint32_t)(seg1 & 1)));
+                if (a1_ready && __all_sync(0xffffffffu, mbar_test(&ffull[f1], f1ph) && mbar_test(&d1empty[d1], d1ph ^ 1))) {
+                    if (leader) {
                         tc_fence_after();
                         const uint64_t fb = fdk + (uint64_t)(f1 * fstep);
                         const uint32_t dd = tD1 + (uint32_t)(d1 * kKlBlockK);
@@ -1441,35 +1456,39 @@ __global__ void __launch_bounds__(kKlThreads)
                             tc_mma_f16(dd, a1d + (uint64_t)(off >> 4), fb + (uint64_t)(offf >> 4), id1, k16 > 0 ? 1u : 0u);
                         }
                         tc_commit(&d1full[d1]);
-                        ring_next(f1, f1ph, p.sf);
-                        ring_next(d1, d1ph, p.nb);
-                        if (++j1 == e1) {
-                            tc_commit(a1empty);  // A1 free once this segment's products are done
-                            seg1++;
-                            a1_ready = false;
-                            if (j1 < nblk) e1 = seg_end_local(j1);
-                        }
-                        did = true;
+                        if (j1 + 1 == e1) tc_commit(a1empty);  // A1 free once this segment's products are done
                     }
-                }
-                if (did) {
-                    spins = 0;
-                    t_idle = 0;
-                } else if (++spins == 256) {  // idle: check the error word and the time limit now and then
-                    spins = 0;
-                    if (*((volatile int *)p.err) != 0) break;
-                    const long long now = clock64();
-                    if (t_idle == 0) {
-                        t_idle = now;
-                    } else if (now - t_idle > kWaitLimitCycles) {
-                        atomicOr(p.err, kErrWaitFull);
-                        break;
+                    __syncwarp();
+                    ring_next(f1, f1ph, p.sf);
+                    ring_next(d1, d1ph, p.nb);
+                    if (++j1 == e1) {
+                        seg1++;
+                        a1_ready = false;
+                        if (j1 < nblk) e1 = seg_end_local(j1);
                     }
+                    did = true;
                 }
             }
+            if (did) {
+                spins = 0;
+                t_idle = 0;
+            } else if (++spins == 256) {  // idle: check the error word and the time limit now and then
+                spins = 0;
+                if (__any_sync(0xffffffffu, *((volatile int *)p.err) != 0)) break;
+                const long long now = __shfl_sync(0xffffffffu, clock64(), 0);
+                if (t_idle == 0) {
+                    t_idle = now;
+                } else if (now - t_idle > kWaitLimitCycles) {
+                    if (leader) atomicOr(p.err, kErrWaitFull);
+                    break;
+                }
+            }
+        }
+        if (leader) {
             tc_commit(mdone);
             mbar_wait_quiet(mdone, 0);
         }
+        __syncwarp();
     } else {
         // finish the denominators (column / row sums of the other factor) from the partials: each of
         // this CTA's entries by all 512 epilogue threads (thread et takes partials et, et + 512, ...,
@@ -1501,70 +1520,60 @@ __global__ void __launch_bounds__(kKlThreads)
                 asm volatile("bar.sync 3, 512;" ::: "memory");
             }
         }
-        const int quarter = warp & 3;           // TMEM lanes this warp may access
-        const int grp = (warp - 2) >> 3;         // group 0 takes even blocks, group 1 odd ones
-        const int part = ((warp - 2) >> 2) & 1;  // which 64 of the block's 128 columns (= V box)
-        const int dpart = (warp - 2) >> 2;       // 0..3: share of the D2 drain
+        const int quarter = warp & 3;     // TMEM lanes this warp may access
+        const int part = (warp - 2) >> 2;  // which 32 of the block's 128 columns; also its share of the D2 drain
         const float eps_pos = fmaxf(p.eps, 1e-30f);
         const int row = quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         int vi = 0, di = 0, seg = 0;
         uint32_t vph = 0, dph = 0;
-        long long g = 0;
         for (long long b = lo; b < hi;) {
             const long long e = seg_end(b);
             bool ok = true;
-            for (long long bb = b; bb < e; bb++, g++) {
-                if ((int)(g & 1) != grp) {  // the other group's block: keep the cursors in step
-                    ring_next(vi, vph, p.sv);
-                    ring_next(di, dph, p.nb);
-                    continue;
-                }
+            // every block by all 16 warps (a quarter of the rows and a quarter of the columns each):
+            // the ratio's latency, on the MMA1 -> MMA2 -> F-release chain, stays short
+            for (long long bb = b; bb < e; bb++) {
                 if (!mbar_wait_sleep(&d1full[di], dph, p.err, kErrWaitTmemFull) ||
                     !mbar_wait_sleep(&vfull[vi], vph, p.err, kErrWaitFull)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const unsigned char *vt = sV(vi) + part * (kKlVBytes / 2);  // this part's 64-column box
-                const uint32_t tb = tD1 + (uint32_t)(di * kKlBlockK + part * 64) + lane_off;
-#pragma unroll
-                for (int h = 0; h < 2; h++) {  // 32 of this warp's 64 columns at a time
-                    float sv[32];
-                    {
-                        float (&s0)[16] = *reinterpret_cast<float (*)[16]>(&sv[0]);
-                        float (&s1)[16] = *reinterpret_cast<float (*)[16]>(&sv[16]);
-                        tmem_ld16(tb + (uint32_t)(h * 32), s0);
-                        tmem_ld16(tb + (uint32_t)(h * 32 + 16), s1);
-                    }
-                    uint4 vraw[4];
-#pragma unroll
-                    for (int cc = 0; cc < 4; cc++) vraw[cc] = *reinterpret_cast<const uint4 *>(vt + sw128(row, h * 4 + cc));
-                    if (h == 1) {  // the V stage is read (the arrive orders the loads before the refill)
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&vempty[vi]);
-                    }
-                    tmem_ld_wait();
-                    uint32_t rr[16];
-#pragma unroll
-                    for (int cc = 0; cc < 4; cc++) {
-                        const __nv_bfloat162 *v2 = reinterpret_cast<const __nv_bfloat162 *>(&vraw[cc]);
-#pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            // R is rounded to BF16 (8-bit significand): the approximate division
-                            // (2 ulp in FP32) is exact enough.  eps_pos > 0 keeps zero-padded
-                            // entries (V = 0, S = 0) at 0.
-                            const float2 vf = __bfloat1622float2(v2[q]);
-                            const float r0 = __fdividef(vf.x, sv[cc * 8 + 2 * q] + eps_pos);
-                            const float r1 = __fdividef(vf.y, sv[cc * 8 + 2 * q + 1] + eps_pos);
-                            const __nv_bfloat162 o = __floats2bfloat162_rn(r0, r1);
-                            rr[cc * 4 + q] = *reinterpret_cast<const uint32_t *>(&o);
-                        }
-                    }
-                    // R (packed pairs) over S columns this warp has already read: half h of the
-                    // part's R goes to its columns 16h .. 16h + 15
-                    tmem_st16(tb + (uint32_t)(h * 16), rr);
+                const uint32_t ta = tD1 + (uint32_t)(di * kKlBlockK + part * 32) + lane_off;
+                float sv[32];
+                {
+                    float (&s0)[16] = *reinterpret_cast<float (*)[16]>(&sv[0]);
+                    float (&s1)[16] = *reinterpret_cast<float (*)[16]>(&sv[16]);
+                    tmem_ld16(ta, s0);
+                    tmem_ld16(ta + 16, s1);
                 }
+                // this part's 32 columns: 64-column box part / 2, 16-byte chunks 4 (part & 1) ..
+                const unsigned char *vt = sV(vi) + (part >> 1) * (kKlVBytes / 2);
+                uint4 vraw[4];
+#pragma unroll
+                for (int cc = 0; cc < 4; cc++) vraw[cc] = *reinterpret_cast<const uint4 *>(vt + sw128(row, (part & 1) * 4 + cc));
+                // the V stage is read (the arrive orders the loads before the producer's refill)
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&vempty[vi]);
+                tmem_ld_wait();
+                uint32_t rr[16];
+#pragma unroll
+                for (int cc = 0; cc < 4; cc++) {
+                    const __nv_bfloat162 *v2 = reinterpret_cast<const __nv_bfloat162 *>(&vraw[cc]);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        // R is rounded to BF16 (8-bit significand): the approximate division
+                        // (2 ulp in FP32) is exact enough.  eps_pos > 0 keeps zero-padded
+                        // entries (V = 0, S = 0) at 0.
+                        const float2 vf = __bfloat1622float2(v2[q]);
+                        const float r0 = __fdividef(vf.x, sv[cc * 8 + 2 * q] + eps_pos);
+                        const float r1 = __fdividef(vf.y, sv[cc * 8 + 2 * q + 1] + eps_pos);
+                        const __nv_bfloat162 o = __floats2bfloat162_rn(r0, r1);
+                        rr[cc * 4 + q] = *reinterpret_cast<const uint32_t *>(&o);
+                    }
+                }
+                // R (packed pairs) over the first 16 of this warp's 32 S columns, already read
+                tmem_st16(ta, rr);
                 tmem_st_wait();
                 tc_fence_before();
                 __syncwarp();
@@ -1576,7 +1585,7 @@ __global__ void __launch_bounds__(kKlThreads)
             if (!mbar_wait_sleep(tfull, (uint32_t)(seg & 1), p.err, kErrWaitTmemFull)) break;
             tc_fence_after();
             float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
-            for (int c = dpart * 16; c < NP; c += 64) {  // the four warps of a quarter take turns by 16 columns
+            for (int c = part * 16; c < NP; c += 64) {  // the four warps of a quarter take turns by 16 columns
                 float v[16];
                 tmem_ld16(tD2 + lane_off + (uint32_t)c, v);
                 tmem_ld_wait();
@@ -2108,13 +2117,14 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
             for (int q = ptr[t]; q < ptr[t + 1]; q++) table[(size_t)t * kSlotW + (q - ptr[t])] = list[q];
     }
     // shared memory: A1 (nbox 16 KB boxes), the F ring (nbox 16 KB boxes a stage), the V ring
-    // (32 KB a stage), barriers.  V stages are split evenly with F's bytes; an F stage is held
-    // longer (until MMA2 of its block completes), so F gets the remainder.
+    // (32 KB a stage), barriers.  An F stage is held from its load until MMA2 of its block
+    // completes (load, MMA1, ratio, MMA2: the longest chain of the pipeline), a V stage only until
+    // the ratio has read it, so F gets at least four stages and V the rest (at least two).
     const int nbox = (npad + 63) / 64;
     const int fbytes = nbox * kKlFBox;
     const int fixed = 1024 + nbox * 16384 + kKlBarBytes;
     const int room = smem_optin() - fixed;
-    const int sv = std::max(2, std::min(kKlMaxSV, room / 2 / kKlVBytes));
+    const int sv = std::max(2, std::min(kKlMaxSV, (room - 4 * fbytes) / kKlVBytes));
     const int sf = std::min(kKlMaxSF, (room - sv * kKlVBytes) / fbytes);
     if (sf < 2 || fixed + sv * kKlVBytes + sf * fbytes > smem_optin()) {
         set_error("KL tensor-core kernel: rank too large for the shared-memory pipeline");
