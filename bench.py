@@ -27,6 +27,7 @@ the summed iterations/s over the max-over-ranks time.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -47,9 +48,12 @@ METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from the committed ncu
 # captures of this workload (one --set full capture per precision, see the profiles
-# directory): tc_gemm_sk_kernel<64> with the update fused in 137.82 MB + 3.61 MB;
+# directory): tc_gemm_sk_kernel<64> with the update fused in 139.85 MB + 3.94 MB;
 # gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
-NCU_TRAFFIC_PER_LAUNCH = {"bf16": 141.43e6, "fp32": 276.09e6}
+NCU_TRAFFIC_PER_LAUNCH = {"bf16": 143.79e6, "fp32": 276.09e6}
+# The same for the KL workload's fused product (tc_kl_gemm_kernel<8>, mean of an H-step and a
+# W-step launch: 140.76 MB + 5.03 MB).
+KL_NCU_TRAFFIC_PER_LAUNCH = {"bf16": 145.79e6}
 
 
 def parse():
@@ -153,6 +157,12 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_started(self, timeout=10.0):
+        """Block until nvidia-smi printed its first sample, so later samples fall in what follows."""
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.01)
+
     def __exit__(self, *exc):
         if self.proc:
             self.proc.terminate()
@@ -187,6 +197,20 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # reference arm / CPU baseline
 # ---------------------------------------------------------------------------
+
+def timed_repeats(measure, dist, clk, min_seconds=1.0, max_reps=500):
+    """Repeat a K-step measurement (measure() returns the device time of exactly K steps, taken with
+    CUDA events and synchronised on both sides) so that the timed loops span at least min_seconds and
+    the clock sampler, started before them, sees them.  Each repetition is the max over ranks; the
+    repetition count comes from the first one (the same on every rank).  Returns the median ms and
+    the spread."""
+    clk.wait_started()
+    first = dist.max(measure())
+    reps = int(min(max_reps, max(1, math.ceil(min_seconds * 1e3 / max(first, 1e-3)))))
+    times = [first] + [dist.max(measure()) for _ in range(reps - 1)]
+    return statistics.median(times), {"repeats": reps, "ms_median": round(statistics.median(times), 4),
+                                      "ms_min": round(min(times), 4), "ms_max": round(max(times), 4)}
+
 
 def euclid_madds(n, m, r):
     # W'V, W'W, W'W H, V H', H H', W H H'  (multiply-adds)
@@ -265,8 +289,13 @@ def run_ours(args, rank, world, local, dist):
     nmf.Synchronize()
     dist.barrier()
     with ClockSampler(local) as clk:
-        t = nmf.TimeIterations(args.steps)
-    ms = dist.max(t["total_ms"])
+        t = {}
+
+        def measure():
+            t.update(nmf.TimeIterations(args.steps))
+            return t["total_ms"]
+
+        ms, rep_info = timed_repeats(measure, dist, clk)
     value = world * args.steps / (ms / 1e3)
     # per-kernel CUDA events around the V-streaming products, in an adjacent loop of the same
     # length on the job's stream (events between kernels would serialise the timed loop above)
@@ -304,7 +333,7 @@ def run_ours(args, rank, world, local, dist):
                       "parallelism": "replicas" if world > 1 else "single",
                       "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16 > 129 MB); no flush" %
                             (n * m * 4 >> 20, n * m * 2 >> 20)},
-           "clocks": clk.summary(), "gpu_launches": t["launches"], "roofline": roofline}
+           "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roofline}
 
     # end to end through the public API from pinned host buffers
     if not args.no_e2e:
@@ -346,15 +375,23 @@ def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world):
         hV, hW, hH = pinned(V), pinned(W), pinned(H)
         oW = pinned(np.zeros_like(W))
         oH = pinned(np.zeros_like(H))
+        from gpumlib_gb300 import _native
+
+        def job(iters):
+            nmf = g.NMF_MultiplicativeEuclidianDistance(hV, hW, hH, eps=eps, precision=precision)
+            for _ in range(iters):
+                nmf.DoIteration()            # per-iteration quality read-back (4 bytes D2H)
+                nmf.QualityImprovement()
+            _native.check(lib.gpunmf_get_w(nmf._h, oW.ctypes.data_as(ctypes.c_void_p)))
+            _native.check(lib.gpunmf_get_h(nmf._h, oH.ctypes.data_as(ctypes.c_void_p)))
+            return nmf
+
+        # one untimed job of `warmup` iterations first: the kernels this path alone uses (quality,
+        # conversions) are loaded on their first launch, which is not part of a job's cost
+        job(max(1, args.warmup)).close()
         dist.barrier()
         t0 = time.perf_counter()
-        nmf = g.NMF_MultiplicativeEuclidianDistance(hV, hW, hH, eps=eps, precision=precision)
-        for _ in range(args.steps):
-            nmf.DoIteration()            # per-iteration quality read-back (4 bytes D2H)
-            nmf.QualityImprovement()
-        from gpumlib_gb300 import _native
-        _native.check(lib.gpunmf_get_w(nmf._h, oW.ctypes.data_as(ctypes.c_void_p)))
-        _native.check(lib.gpunmf_get_h(nmf._h, oH.ctypes.data_as(ctypes.c_void_p)))
+        nmf = job(args.steps)
         dt = time.perf_counter() - t0
         nmf.close()
         dt = dist.max(dt)
@@ -362,8 +399,9 @@ def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world):
         d2h = W.nbytes + H.nbytes + 4 * args.steps
         return {"value": round(world * args.steps / dt, 2), "unit": "iters/s",
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
-                "note": "one job of %d iterations from pinned host buffers: create (H2D V,W,H), iterations with "
-                        "quality read-back, GetW/GetH (D2H); bytes amortised per step" % args.steps}
+                "note": "one job of %d iterations from pinned host buffers, after one untimed warm-up job: create "
+                        "(H2D V,W,H), iterations with quality read-back, GetW/GetH (D2H); bytes amortised per step"
+                        % args.steps}
     finally:
         for p in bufs:
             lib.gpunmf_host_free(p)
@@ -464,8 +502,13 @@ def run_kl(args, rank, world, local, dist):
     nmf.Synchronize()
     dist.barrier()
     with ClockSampler(local) as clk:
-        t = nmf.TimeIterations(args.steps)
-    ms = dist.max(t["total_ms"])
+        t = {}
+
+        def measure():
+            t.update(nmf.TimeIterations(args.steps))
+            return t["total_ms"]
+
+        ms, rep_info = timed_repeats(measure, dist, clk)
     value = world * args.steps / (ms / 1e3)
     tk = nmf.TimeIterations(args.steps, kernel_timing=True)
     nmf.close()
@@ -481,7 +524,7 @@ def run_kl(args, rank, world, local, dist):
                 "frac": round(tfs / bf16_tf, 4)}
     else:
         roof = {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s", "frac": round(gbs / hbm, 4)}
-    roof.update({"traffic": None, "peak_source": src, "avg_launch_ms": round(avg_ms, 5),
+    roof.update({"traffic": KL_NCU_TRAFFIC_PER_LAUNCH.get(prec), "peak_source": src, "avg_launch_ms": round(avg_ms, 5),
                  "kernel": "fused KL product (S = WH -> V/(S+eps) -> numerator)" if prec == "bf16" else
                            "KL ratio SGEMM", "hbm_frac": round(gbs / hbm, 4),
                  "tensor_frac": round(tfs / bf16_tf, 4) if prec == "bf16" else None})
@@ -492,7 +535,7 @@ def run_kl(args, rank, world, local, dist):
            "config": {"workload": "kl_counts_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r, "rule": "kl",
                       "precision": prec, "eps": eps, "zero_fraction": float(np.mean(V == 0)),
                       "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16)" % (n * m * 4 >> 20, n * m * 2 >> 20)},
-           "clocks": clk.summary(), "gpu_launches": t["launches"], "roofline": roof}
+           "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roof}
     if args.full_job_iters and rank == 0:
         iters = min(args.full_job_iters, cfg["iters"])
         res = {}

@@ -50,6 +50,25 @@ def test_kl_one_iteration_matches_emulation(gpu, shape):
     assert rel(W1g, W1) <= 2e-5, "W-step (fused KL tcgen05) differs"
 
 
+@pytest.mark.parametrize("shape", [(129, 65, 1), (300, 1300, 7), (1000, 777, 20)], ids=["129x65r1", "300x1300r7", "1000x777r20"])
+def test_kl_tiny_eps_matches_emulation(gpu, shape):
+    """eps = 1e-30: in the zero-padded rows and columns of a tile (S = 0) a pair's product of
+    S + eps underflows, so the kernel's one-reciprocal-per-pair step must fall back to plain
+    divisions there; any inf or NaN it let through would reach the numerators."""
+    n, m, r = shape
+    g = np.random.Generator(np.random.PCG64(3 * n + m + r))
+    V = np.asfortranarray(g.poisson(2.0, size=(n, m)).astype(np.float32))
+    W, H = inputs.factors(190 + n, n, m, r)
+    eps = np.float32(1e-30)
+    with gpu.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision="bf16", quality_interval=0) as nmf:
+        nmf.DoIteration()
+        W1g, H1g = nmf.GetW(), nmf.GetH()
+    assert np.isfinite(W1g).all() and np.isfinite(H1g).all()
+    W1, H1 = emulate_kl_one(V, W, H, float(eps), H1g)
+    assert rel(H1g, H1) <= 2e-5, "H-step (fused KL tcgen05) differs"
+    assert rel(W1g, W1) <= 2e-5, "W-step (fused KL tcgen05) differs"
+
+
 def test_kl_bf16_tracks_fp32(gpu):
     n, m, r = 2048, 1536, 64
     g = np.random.Generator(np.random.PCG64(7))
