@@ -2490,22 +2490,79 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
     return GPUNMF_OK;
 }
 
+static cudaError_t launch_gemm_cfg(TcGemm &g, cudaLaunchConfig_t &cfg) {
+    switch (g.fnp) {
+        case 32: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<32>, g.tmA, g.tmB, g.p);
+        case 64: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<64>, g.tmA, g.tmB, g.p);
+        default: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<0>, g.tmA, g.tmB, g.p);
+    }
+}
+
+// The stream of the last fused-update launch per device (see launch_gemm); a job that is torn down
+// (its stream drained first) forgets its stream here.
+struct LastFused {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    bool used = false;
+    cudaEvent_t ev = nullptr;
+};
+static LastFused g_last_fused[64];
+
+static void forget_fused_stream(cudaStream_t s) {
+    for (LastFused &L : g_last_fused) {
+        std::lock_guard<std::mutex> lock(L.mu);
+        if (L.used && L.stream == s) L.used = false;
+    }
+}
+
 static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.grid);
     cfg.blockDim = dim3(gemm_threads(g.fnp));
     cfg.dynamicSmemBytes = g.smem;
     cfg.stream = s;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    switch (g.fnp) {
-        case 32: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<32>, g.tmA, g.tmB, g.p);
-        case 64: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<64>, g.tmA, g.tmB, g.p);
-        default: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<0>, g.tmA, g.tmB, g.p);
+    if (!g.fnp) return launch_gemm_cfg(g, cfg);
+    // The fused update's CTAs wait on one another (tile arrivals, the Gram assembly; every wait is
+    // bounded), so its grid (at most one CTA per SM) must be resident at once.  On one stream that
+    // holds: the previous kernel's CTAs never wait on the next one.  Two fused grids on different
+    // streams could each hold part of the SMs and wait for the rest, so:
+    //  - a launch being captured into a graph (the server's iteration chunks, replayed on many
+    //    streams) is cooperative, which makes the residency of its grid a launch condition;
+    //  - otherwise fused launches of this process are serialised across streams (a launch on a
+    //    stream other than the last one's first waits for everything submitted to that stream),
+    //    which keeps the programmatic dependent launch that a cooperative launch forgoes (~6% per
+    //    iteration).
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) return e;
+    if (cap != cudaStreamCaptureStatusNone) {
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        return launch_gemm_cfg(g, cfg);
     }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    LastFused &L = g_last_fused[dev & 63];
+    std::lock_guard<std::mutex> lock(L.mu);
+    cudaStreamCaptureStatus lcap = cudaStreamCaptureStatusNone;
+    if (L.used && L.stream != s && cudaStreamIsCapturing(L.stream, &lcap) == cudaSuccess &&
+        lcap == cudaStreamCaptureStatusNone) {  // (work being captured there is not running yet)
+        if (!L.ev) {
+            e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
+        e = cudaEventRecord(L.ev, L.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, L.ev, 0);
+        if (e != cudaSuccess) return e;
+    }
+    L.stream = s;
+    L.used = true;
+    return launch_gemm_cfg(g, cfg);
 }
 
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
@@ -2579,6 +2636,7 @@ gpunmf_status tc_check(gpunmf_job *j) {
 void tc_destroy(gpunmf_job *j) {
     TcState *t = j->tc;
     if (!t) return;
+    if (t->gh.fnp) forget_fused_stream(j->stream);
     void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h, t->G_w, t->GP_h, t->GP_w,
                     t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list,
                     t->gh.tile_slots, t->gw.tile_slots, t->Wr, t->Hc, t->S_w, t->S_h, t->SP_w, t->SP_h,
