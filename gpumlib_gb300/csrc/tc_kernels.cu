@@ -1250,6 +1250,14 @@ constexpr int kKlFBox = kKlBlockK * 128;  // 16 KB: 128 K-rows x 64 columns of t
 constexpr int kKlMaxSV = 6, kKlMaxSF = 8, kKlMaxNB = 3;
 constexpr int kKlBarBytes = 1024;  // barriers, the TMEM address, the denominator scratch
 
+// The hardware's approximate reciprocal (rcp.approx.ftz.f32, about 1 ulp): the ratio is rounded to
+// BF16 afterwards, so this is exact enough, and it is a single special-function operation.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ uint32_t sw128(int row, int chunk) {
     return (uint32_t)(row * 128 + ((chunk ^ (row & 7)) << 4));
 }
@@ -1279,15 +1287,13 @@ __global__ void __launch_bounds__(kKlThreads)
     constexpr int NP = NK * 16;
     const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
     const int fBytes = p.nbox * kKlFBox;
-    unsigned char *sA1 = reinterpret_cast<unsigned char *>(base);
-    unsigned char *sFr = sA1 + p.nbox * 16384;
+    unsigned char *sFr = reinterpret_cast<unsigned char *>(base);
     unsigned char *sVr = sFr + p.sf * fBytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(sVr + p.sv * kKlVBytes);
     uint64_t *vfull = bars, *vempty = vfull + kKlMaxSV;
     uint64_t *ffull = vempty + kKlMaxSV, *fempty = ffull + kKlMaxSF;
     uint64_t *d1full = fempty + kKlMaxSF, *d1empty = d1full + kKlMaxNB, *rfull = d1empty + kKlMaxNB;
-    uint64_t *a1full = rfull + kKlMaxNB, *a1empty = a1full + 1;
-    uint64_t *tfull = a1empty + 1, *tempty = tfull + 1;
+    uint64_t *tfull = rfull + kKlMaxNB, *tempty = tfull + 1;
     uint64_t *mdone = tempty + 1;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
     float *red = reinterpret_cast<float *>(mdone + 2);  // [16] per-warp sums of the denominators
@@ -1314,8 +1320,6 @@ __global__ void __launch_bounds__(kKlThreads)
             mbar_init(&d1empty[b], 1);
             mbar_init(&rfull[b], kKlEpiWarps);
         }
-        mbar_init(a1full, 1);
-        mbar_init(a1empty, 1);
         mbar_init(tfull, 1);
         mbar_init(tempty, kKlEpiWarps);
         mbar_init(mdone, 1);
@@ -1332,8 +1336,9 @@ __global__ void __launch_bounds__(kKlThreads)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    // TMEM columns: the numerator accumulator [0, npad), then nb S/R buffers of 128
-    const uint32_t tD2 = tmem, tD1 = tmem + (uint32_t)NP;
+    // TMEM columns: the numerator accumulator [0, npad), A1 (the tile's factor rows, BF16 pairs)
+    // [npad, npad + 64), then nb S/R buffers of 128
+    const uint32_t tD2 = tmem, tA1 = tmem + (uint32_t)NP, tD1 = tmem + (uint32_t)(NP + 64);
     griddep_wait();
     griddep_launch_dependents();
 
@@ -1347,10 +1352,15 @@ __global__ void __launch_bounds__(kKlThreads)
             for (long long b = lo; b < hi && ok;) {
                 const int t = (int)(b / p.kblocks);
                 const long long e = seg_end(b);
-                // the factor tile of this row tile (MMA1's A), once per segment
-                if (!mbar_wait_sleep(a1empty, (uint32_t)((seg & 1) ^ 1), p.err, kErrWaitEmpty)) break;
-                mbar_arrive_expect_tx(a1full, (uint32_t)(p.nbox * 16384));
-                for (int q = 0; q < p.nbox; q++) tma_load_2d(sA1 + q * 16384, &tmA1, q * 64, t * kTileM, a1full);
+                // the factor rows of this row tile (MMA1's A), once per segment, as an entry of the F
+                // ring (same size: nbox boxes of 128 rows x 64 columns); the MMA thread copies it
+                // into TMEM and frees the entry
+                if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty)) break;
+                mbar_arrive_expect_tx(&ffull[fi], (uint32_t)fBytes);
+                for (int q = 0; q < p.nbox; q++) tma_load_2d(sF(fi) + q * kKlFBox, &tmA1, q * 64, t * kTileM, &ffull[fi]);
+                armed_f |= 1u << fi;
+                par_f = (par_f & ~(1u << fi)) | (fph << fi);
+                ring_next(fi, fph, p.sf);
                 for (long long bb = b; bb < e; bb++) {
                     const int k0 = (int)(bb % p.kblocks) * kKlBlockK;
                     if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty)) {
@@ -1382,7 +1392,6 @@ __global__ void __launch_bounds__(kKlThreads)
                 if (armed_f >> s & 1) mbar_wait_quiet(&ffull[s], par_f >> s & 1);
             for (int s = 0; s < p.sv; s++)
                 if (armed_v >> s & 1) mbar_wait_quiet(&vfull[s], par_v >> s & 1);
-            if (seg > 0) mbar_wait_quiet(a1full, (uint32_t)((seg - 1) & 1));
         }
     } else if (warp == 1) {
         // The whole warp runs the MMA loop (its state is warp-uniform, barrier tests are voted), and
@@ -1393,7 +1402,6 @@ __global__ void __launch_bounds__(kKlThreads)
         // descriptors of A1 and of F stage 0 (K-major for MMA1, MN-major for MMA2: the factor's
         // 64-column boxes are the MN chunks, 16 KB apart); a stage or a K step moves the start
         // address, which is the descriptor's low bits (address >> 4)
-        const uint64_t a1d = smem_desc(smem_u32(sA1), 16, 1024, 2);
         const uint64_t fdk = smem_desc(smem_u32(sFr), 16, 1024, 2);
         const uint64_t fdm = smem_desc(smem_u32(sFr), kKlFBox, 1024, 2);
         const uint32_t fstep = (uint32_t)fBytes >> 4;
@@ -1401,13 +1409,15 @@ __global__ void __launch_bounds__(kKlThreads)
         // blocks of this CTA counted from 0; a segment ends at a tile boundary
         const int nblk = (int)(hi - lo);
         auto seg_end_local = [&](int j) { return (int)(seg_end(lo + j) - lo); };
-        // MMA1 cursor: block j1, its F stage and S/R buffer, its segment
-        int j1 = 0, e1 = seg_end_local(0), f1 = 0, d1 = 0, seg1 = 0;
+        // MMA1 cursor: block j1, its F-ring entry and S/R buffer; need_a1: the next entry is the A1
+        // of a new segment (each segment's entries are its A1, then one F per block)
+        int j1 = 0, e1 = seg_end_local(0), f1 = 0, d1 = 0;
         uint32_t f1ph = 0, d1ph = 0;
-        bool a1_ready = false;
-        // MMA2 cursor
+        bool need_a1 = true;
+        // MMA2 cursor (starts past the first segment's A1 entry)
         int j2 = 0, e2 = e1, f2 = 0, d2 = 0, seg2 = 0;
         uint32_t f2ph = 0, d2ph = 0;
+        ring_next(f2, f2ph, p.sf);
         bool first2 = true;
         long long t_idle = 0;
         int spins = 0;
@@ -1438,32 +1448,51 @@ __global__ void __launch_bounds__(kKlThreads)
                 if (++j2 == e2) {
                     seg2++;
                     first2 = true;
-                    if (j2 < nblk) e2 = seg_end_local(j2);
+                    if (j2 < nblk) {
+                        e2 = seg_end_local(j2);
+                        ring_next(f2, f2ph, p.sf);  // past the next segment's A1 entry
+                    }
                 }
                 did = true;
             }
-            // MMA1 of the next block once its F tile, a free S/R buffer and its A1 are there
-            if (j1 < nblk) {
-                if (!a1_ready) a1_ready = __all_sync(0xffffffffu, mbar_test(a1full, (uint32_t)(seg1 & 1)));
-                if (a1_ready && __all_sync(0xffffffffu, mbar_test(&ffull[f1], f1ph) && mbar_test(&d1empty[d1], d1ph ^ 1))) {
+            // A1 of a new segment: copied from its F-ring entry into TMEM.  The copy is ordered after
+            // the previous segment's MMA1s (which read the old A1) and before the new ones, like
+            // another MMA of this thread; the entry is freed when it has completed.
+            if (j1 < nblk && need_a1 && __all_sync(0xffffffffu, mbar_test(&ffull[f1], f1ph))) {
+                if (leader) {
+                    tc_fence_after();
+                    const uint64_t ad = fdk + (uint64_t)(f1 * fstep);
+#pragma unroll
+                    for (int k16 = 0; k16 < NK; k16++) {
+                        const int off = (k16 >> 2) * kKlFBox + (k16 & 3) * 32;
+                        tc_cp_128x256b(tA1 + (uint32_t)(k16 * 8), ad + (uint64_t)(off >> 4));
+                    }
+                    tc_commit(&fempty[f1]);
+                }
+                __syncwarp();
+                ring_next(f1, f1ph, p.sf);
+                need_a1 = false;
+                did = true;
+            }
+            // MMA1 of the next block once its F tile and a free S/R buffer are there
+            if (j1 < nblk && !need_a1) {
+                if (__all_sync(0xffffffffu, mbar_test(&ffull[f1], f1ph) && mbar_test(&d1empty[d1], d1ph ^ 1))) {
                     if (leader) {
                         tc_fence_after();
                         const uint64_t fb = fdk + (uint64_t)(f1 * fstep);
                         const uint32_t dd = tD1 + (uint32_t)(d1 * kKlBlockK);
 #pragma unroll
                         for (int k16 = 0; k16 < NK; k16++) {
-                            const int off = (k16 >> 2) * 16384 + (k16 & 3) * 32, offf = (k16 >> 2) * kKlFBox + (k16 & 3) * 32;
-                            tc_mma_f16(dd, a1d + (uint64_t)(off >> 4), fb + (uint64_t)(offf >> 4), id1, k16 > 0 ? 1u : 0u);
+                            const int offf = (k16 >> 2) * kKlFBox + (k16 & 3) * 32;
+                            tc_mma_f16_ts(dd, tA1 + (uint32_t)(k16 * 8), fb + (uint64_t)(offf >> 4), id1, k16 > 0 ? 1u : 0u);
                         }
                         tc_commit(&d1full[d1]);
-                        if (j1 + 1 == e1) tc_commit(a1empty);  // A1 free once this segment's products are done
                     }
                     __syncwarp();
                     ring_next(f1, f1ph, p.sf);
                     ring_next(d1, d1ph, p.nb);
                     if (++j1 == e1) {
-                        seg1++;
-                        a1_ready = false;
+                        need_a1 = true;
                         if (j1 < nblk) e1 = seg_end_local(j1);
                     }
                     did = true;
@@ -1472,8 +1501,11 @@ __global__ void __launch_bounds__(kKlThreads)
             if (did) {
                 spins = 0;
                 t_idle = 0;
-            } else if (++spins == 256) {  // idle: check the error word and the time limit now and then
-                spins = 0;
+            } else if (++spins & 255) {
+                // idle: back off a little, leaving this SM sub-partition's issue slots to the ratio
+                // warps that share it (a wake-up costs at most the back-off)
+                __nanosleep(32);
+            } else {  // now and then: the error word and the time limit
                 if (__any_sync(0xffffffffu, *((volatile int *)p.err) != 0)) break;
                 const long long now = __shfl_sync(0xffffffffu, clock64(), 0);
                 if (t_idle == 0) {
@@ -1562,12 +1594,11 @@ __global__ void __launch_bounds__(kKlThreads)
                     const __nv_bfloat162 *v2 = reinterpret_cast<const __nv_bfloat162 *>(&vraw[cc]);
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
-                        // R is rounded to BF16 (8-bit significand): the approximate division
-                        // (2 ulp in FP32) is exact enough.  eps_pos > 0 keeps zero-padded
-                        // entries (V = 0, S = 0) at 0.
+                        // eps_pos > 0 keeps zero-padded entries (V = 0, S = 0) at 0: 1/eps_pos is
+                        // finite for eps_pos >= 1e-30.
                         const float2 vf = __bfloat1622float2(v2[q]);
-                        const float r0 = __fdividef(vf.x, sv[cc * 8 + 2 * q] + eps_pos);
-                        const float r1 = __fdividef(vf.y, sv[cc * 8 + 2 * q + 1] + eps_pos);
+                        const float r0 = vf.x * rcp_approx(sv[cc * 8 + 2 * q] + eps_pos);
+                        const float r1 = vf.y * rcp_approx(sv[cc * 8 + 2 * q + 1] + eps_pos);
                         const __nv_bfloat162 o = __floats2bfloat162_rn(r0, r1);
                         rr[cc * 4 + q] = *reinterpret_cast<const uint32_t *>(&o);
                     }
@@ -2122,7 +2153,7 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
     // the ratio has read it, so F gets at least four stages and V the rest (at least two).
     const int nbox = (npad + 63) / 64;
     const int fbytes = nbox * kKlFBox;
-    const int fixed = 1024 + nbox * 16384 + kKlBarBytes;
+    const int fixed = 1024 + kKlBarBytes;
     const int room = smem_optin() - fixed;
     const int sv = std::max(2, std::min(kKlMaxSV, (room - 4 * fbytes) / kKlVBytes));
     const int sf = std::min(kKlMaxSF, (room - sv * kKlVBytes) / fbytes);
@@ -2137,7 +2168,7 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
     g.p.nbox = nbox;
     g.p.sv = sv;
     g.p.sf = sf;
-    g.p.nb = std::min(kKlMaxNB, (512 - npad) / kKlBlockK);  // S/R buffers beside the accumulator
+    g.p.nb = std::min(kKlMaxNB, (512 - npad - 64) / kKlBlockK);  // S/R buffers beside the accumulator and A1
     g.p.eps = j->eps;
     g.p.err = err;
     g.smem = fixed + sv * kKlVBytes + sf * fbytes;
