@@ -52,8 +52,8 @@ METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
 # gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
 NCU_TRAFFIC_PER_LAUNCH = {"bf16": 143.79e6, "fp32": 276.09e6}
 # The same for the KL workload's fused product (tc_kl_gemm_kernel<8>, mean of an H-step and a
-# W-step launch: 140.76 MB + 5.03 MB).
-KL_NCU_TRAFFIC_PER_LAUNCH = {"bf16": 145.79e6}
+# W-step launch: 140.72 MB + 4.67 MB).
+KL_NCU_TRAFFIC_PER_LAUNCH = {"bf16": 145.39e6}
 
 
 def parse():
