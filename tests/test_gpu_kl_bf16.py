@@ -32,7 +32,9 @@ def emulate_kl_one(V, W, H, eps, H1_gpu):
 
 
 SHAPES = [(512, 384, 16), (1000, 777, 20), (300, 1300, 7), (129, 65, 1), (2048, 1024, 128), (513, 700, 100),
-          (64, 4096, 64), (37, 11, 3)]
+          (64, 4096, 64), (37, 11, 3),
+          # ranks whose padded width (48, 80, 96) fills the factor tile's second 64-column box only in part
+          (700, 900, 40), (1030, 640, 70), (400, 1500, 90)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=["%dx%dr%d" % s for s in SHAPES])
