@@ -284,9 +284,14 @@ static gpunmf_status quality_step(gpunmf_job *j, bool fused_wh) {
     cudaStream_t s = j->stream;
     int n = j->n, m = j->m, r = j->r;
     if (j->precision == GPUNMF_BF16 && tc_quality_ready(j)) {
-        // BF16 jobs: W H on the tensor cores from the BF16 factors, V as BF16
+        // BF16 jobs: W H on the tensor cores from the BF16 factors, V as BF16; one launch that also
+        // writes the value into the pinned read-back word where the device can reach it
         TRY_STATUS(tc_quality(j));
-        j->launches -= 2;  // counted there
+        if (!tc_quality_writes_host(j))
+            GPUNMF_CUDA_TRY(cudaMemcpyAsync(j->h_quality(), j->d_quality, sizeof(float), cudaMemcpyDeviceToHost, s));
+        GPUNMF_CUDA_TRY(cudaEventRecord(j->qev, s));
+        j->q_pending = true;
+        return GPUNMF_OK;
     } else if (fused_wh) {
         GPUNMF_CUDA_TRY(wh_quality_f32(n, m, r, j->W, j->H, j->V, j->eps, j->red, s));
         GPUNMF_CUDA_TRY(finalize_partials(j->red, wh_reduce_ctas(n, m), 1, 0, j->d_quality, nullptr, s));

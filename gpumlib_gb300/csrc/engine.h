@@ -86,6 +86,8 @@ gpunmf_status tc_prepare(gpunmf_job *j);  // after V/W/H are uploaded
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW);
 // quality of the current factors on the tensor cores (BF16 jobs with npad <= 128)
 bool tc_quality_ready(const gpunmf_job *j);
+// whether the tensor-core quality kernel writes the job's pinned read-back word itself
+bool tc_quality_writes_host(const gpunmf_job *j);
 gpunmf_status tc_quality(gpunmf_job *j);
 gpunmf_status tc_check(gpunmf_job *j);    // reads the kernels' error word (after a sync)
 void tc_destroy(gpunmf_job *j);

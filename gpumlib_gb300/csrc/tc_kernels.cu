@@ -744,18 +744,23 @@ constexpr int kQTile = 128;
 constexpr int kQVBytes = kQTile * kQTile * 2;
 
 struct QParams {
-    int tiles_i, tiles_u, nbox, npad, stages;
+    int tiles_i, tiles_u, npad, stages;
     float eps;
     double *partial;  // [grid]
     int *err;
+    int *done;        // CTAs finished (the last one sums the partials and resets it)
+    float *out;       // the quality (device)
+    float *out_host;  // the job's pinned read-back word, written directly where the device can (else null)
 };
 
 __global__ void __launch_bounds__(kQThreads, 1)
     tc_quality_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ CUtensorMap tmV, QParams p) {
     const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
-    const int boxBytes = kQTile * kBlockK * 2;  // one 128 x 64 BF16 box (16 KB)
-    const int stageBytes = 2 * p.nbox * boxBytes + kQVBytes;
+    // factor tiles MN-major, straight from the BF16 copies the iterations keep (Wb column-major: rows i
+    // contiguous; Hb row-major: columns u contiguous): two 64-wide boxes of npad K-rows each
+    const int boxBytes = p.npad * 128;
+    const int stageBytes = 4 * boxBytes + kQVBytes;
     unsigned char *ring = reinterpret_cast<unsigned char *>(base);
     uint64_t *full = reinterpret_cast<uint64_t *>(ring + p.stages * stageBytes);
     uint64_t *empty = full + p.stages;
@@ -765,8 +770,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
     double *red = reinterpret_cast<double *>(tmem_slot + 2);  // [2][kQEpiWarps], 8-byte aligned
     auto sA = [&](int st) { return ring + st * stageBytes; };
-    auto sB = [&](int st) { return ring + st * stageBytes + p.nbox * boxBytes; };
-    auto sV = [&](int st) { return reinterpret_cast<const __nv_bfloat16 *>(ring + st * stageBytes + 2 * p.nbox * boxBytes); };
+    auto sB = [&](int st) { return ring + st * stageBytes + 2 * boxBytes; };
+    auto sV = [&](int st) { return reinterpret_cast<const __nv_bfloat16 *>(ring + st * stageBytes + 4 * boxBytes); };
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int T = p.tiles_i * p.tiles_u;
@@ -793,6 +798,9 @@ __global__ void __launch_bounds__(kQThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // the factors are read only after the kernel that wrote them has completed
+    griddep_wait();
+    griddep_launch_dependents();
 
     if (warp == 0) {
         if (lane == 0) {
@@ -803,9 +811,9 @@ __global__ void __launch_bounds__(kQThreads, 1)
                 const int ti = t / p.tiles_u, tu = t % p.tiles_u;
                 if (!mbar_wait(&empty[st], ph ^ 1, p.err, kErrWaitEmpty)) break;
                 mbar_arrive_expect_tx(&full[st], (uint32_t)stageBytes);
-                for (int q = 0; q < p.nbox; q++) {
-                    tma_load_2d(sA(st) + q * boxBytes, &tmA, q * kBlockK, ti * kQTile, &full[st]);
-                    tma_load_2d(sB(st) + q * boxBytes, &tmB, q * kBlockK, tu * kQTile, &full[st]);
+                for (int q = 0; q < 2; q++) {
+                    tma_load_2d(sA(st) + q * boxBytes, &tmA, ti * kQTile + q * 64, 0, &full[st]);
+                    tma_load_2d(sB(st) + q * boxBytes, &tmB, tu * kQTile + q * 64, 0, &full[st]);
                 }
                 for (int q = 0; q < 2; q++)  // V' tile: rows i, 64 columns u per box
                     tma_load_2d(const_cast<__nv_bfloat16 *>(sV(st)) + q * (kQTile * 64), &tmV, tu * kQTile + q * 64,
@@ -822,7 +830,9 @@ __global__ void __launch_bounds__(kQThreads, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16_f32(kQTile, kQTile);
+            // both operands MN-major: a K16 step is 16 rows of 128 bytes; the second 64-wide box of M / N
+            // is boxBytes further (leading byte offset), 8-row groups 1024 bytes apart
+            const uint32_t idesc = idesc_bf16_f32(kQTile, kQTile) | kIdescAMnMajor | kIdescBMnMajor;
             int st = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             for (int t = blockIdx.x; t < T; t += gridDim.x) {
@@ -830,11 +840,9 @@ __global__ void __launch_bounds__(kQThreads, 1)
                 if (!mbar_wait(&full[st], ph, p.err, kErrWaitFull)) break;
                 tc_fence_after();
                 const uint32_t a0 = smem_u32(sA(st)), b0 = smem_u32(sB(st));
-                for (int k16 = 0; k16 < p.npad / 16; k16++) {
-                    const int q = k16 >> 2, w = (k16 & 3) * 32;
-                    tc_mma_f16(tmem + (uint32_t)(acc * kQTile), smem_desc(a0 + q * boxBytes + w, 16, 1024, 2),
-                               smem_desc(b0 + q * boxBytes + w, 16, 1024, 2), idesc, k16 > 0 ? 1u : 0u);
-                }
+                for (int k16 = 0; k16 < p.npad / 16; k16++)
+                    tc_mma_f16(tmem + (uint32_t)(acc * kQTile), smem_desc(a0 + k16 * 2048, boxBytes, 1024, 2),
+                               smem_desc(b0 + k16 * 2048, boxBytes, 1024, 2), idesc, k16 > 0 ? 1u : 0u);
                 tc_commit(&empty[st]);
                 tc_commit(&tfull[acc]);
                 if (++st == p.stages) {
@@ -929,6 +937,26 @@ __global__ void __launch_bounds__(kQThreads, 1)
             sm += red[kQEpiWarps + w];
         }
         p.partial[blockIdx.x] = 0.30102999566398120 * l - sm;  // log10(x) = log2(x) log10(2)
+        __threadfence();
+        reinterpret_cast<volatile int *>(red)[0] = atomicAdd(p.done, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (warp == 0 && reinterpret_cast<volatile int *>(red)[0]) {
+        // the last CTA: the partials summed in CTA order (lane-strided, then a fixed tree), so the
+        // value does not depend on which CTA finished last
+        __threadfence();
+        double q = 0.0;
+        for (int c = lane; c < (int)gridDim.x; c += 32) q += __ldcg(p.partial + c);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) q += __shfl_down_sync(0xffffffffu, q, off);
+        if (lane == 0) {
+            p.out[0] = (float)q;
+            if (p.out_host) {
+                p.out_host[0] = (float)q;
+                __threadfence_system();
+            }
+            *p.done = 0;
+        }
     }
     if (warp == 0) {
         tc_fence_after();
@@ -2304,30 +2332,34 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
     TcState *t = j->tc;
     if (t->npad > 128) return GPUNMF_OK;  // the FP32 quality kernel serves larger ranks
     const int n = j->n, m = j->m, r = j->r;
-    if (!t->Wr) {  // Euclidean jobs: the K-major copies are made when the quality is sampled
-        t->ldr = t->npad;
-        cudaError_t e = job_dev_alloc(j, (void **)&t->Wr, (size_t)n * t->ldr * 2);
-        if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hc, (size_t)m * t->ldr * 2);
-        if (e != cudaSuccess) {
-            set_error("quality buffers: %s", cudaGetErrorString(e));
-            cudaGetLastError();
-            return GPUNMF_ERR_NOMEM;
-        }
-    }
     QParams &q = t->qp;
     q.tiles_i = ceil_div(n, kQTile);
     q.tiles_u = ceil_div(m, kQTile);
-    q.nbox = ceil_div(t->npad, kBlockK);
     q.npad = t->npad;
     q.eps = j->eps;
     q.err = t->err;
-    const int stageBytes = 2 * q.nbox * kQTile * kBlockK * 2 + kQVBytes;
+    q.out = j->d_quality;
+    {
+        cudaError_t e = job_dev_alloc(j, (void **)&q.done, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(q.done, 0, sizeof(int), j->stream);
+        if (e != cudaSuccess) {
+            set_error("quality counter: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            return GPUNMF_ERR_NOMEM;
+        }
+        // the pinned read-back word, where the device can write it directly (mapped host memory)
+        void *dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, j->h_quality(), 0) == cudaSuccess) q.out_host = static_cast<float *>(dp);
+        cudaGetLastError();
+    }
+    const int stageBytes = 4 * t->npad * 128 + kQVBytes;
     q.stages = std::min(3, (smem_optin() - 1024 - 256) / stageBytes);
     t->qsmem = 1024 + q.stages * stageBytes + (2 * q.stages + 5) * 8 + 8 + 2 * kQEpiWarps * 8 + 16;
     t->qgrid = (int)std::min<long long>(num_sms(), (long long)q.tiles_i * q.tiles_u);
     if (q.stages < 2 || (size_t)t->qgrid > j->red_cap) return GPUNMF_OK;  // not worth it here
-    gpunmf_status st = make_map(&t->tmQA, t->Wr, r, n, t->ldr, kQTile);
-    if (st == GPUNMF_OK) st = make_map(&t->tmQB, t->Hc, r, m, t->ldr, kQTile);
+    // Wb: {i, a}, Hb: {u, a}; boxes of 64 (contiguous) x npad (K rows; rows past r read zeros)
+    gpunmf_status st = make_map(&t->tmQA, t->Wb, n, r, t->ldw, t->npad);
+    if (st == GPUNMF_OK) st = make_map(&t->tmQB, t->Hb, m, r, t->ldh, t->npad);
     if (st == GPUNMF_OK) st = make_map(&t->tmQV, t->Vbt, m, n, t->ldvt, kQTile);  // V': {u, i}, box {64, 128}
     if (st != GPUNMF_OK) return st;
     static std::once_flag once;
@@ -2344,22 +2376,23 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
 }
 
 bool tc_quality_ready(const gpunmf_job *j) { return j->tc && j->tc->qp.partial != nullptr; }
+bool tc_quality_writes_host(const gpunmf_job *j) { return j->tc && j->tc->qp.out_host != nullptr; }
 
 // The quality of the current factors into j->d_quality (float), as the FP32 path leaves it.
 gpunmf_status tc_quality(gpunmf_job *j) {
     TcState *t = j->tc;
-    cudaStream_t s = j->stream;
-    if (!rule_is_kl(j->rule)) {  // Euclidean jobs keep only Wb / Hb current: make the K-major copies
-        convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->n * t->ldr, 256)), 256, 0, s>>>(
-            j->W, j->n, j->r, j->n, true, t->Wr, t->ldr);
-        convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->m * t->ldr, 256)), 256, 0, s>>>(
-            j->H, j->m, j->r, 0, false, t->Hc, t->ldr);
-        j->launches += 2;
-    }
-    tc_quality_kernel<<<t->qgrid, kQThreads, t->qsmem, s>>>(t->tmQA, t->tmQB, t->tmQV, t->qp);
-    GPUNMF_CUDA_TRY(cudaGetLastError());
-    GPUNMF_CUDA_TRY(finalize_partials(j->red, t->qgrid, 1, 0, j->d_quality, nullptr, s));
-    j->launches += 2;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(t->qgrid);
+    cfg.blockDim = dim3(kQThreads);
+    cfg.dynamicSmemBytes = t->qsmem;
+    cfg.stream = j->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GPUNMF_CUDA_TRY(cudaLaunchKernelEx(&cfg, tc_quality_kernel, t->tmQA, t->tmQB, t->tmQV, t->qp));
+    j->launches += 1;
     return GPUNMF_OK;
 }
 

@@ -264,7 +264,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
            | ((uint32_t)(N >> 3) << 17)      // N / 8
            | ((uint32_t)(M >> 4) << 24);     // M / 16
 }
-// Instruction-descriptor bit: the B operand is MN-major (N contiguous in each 128-byte row).
+// Instruction-descriptor bits: the A / B operand is MN-major (M / N contiguous in each 128-byte row).
+constexpr uint32_t kIdescAMnMajor = 1u << 15;
 constexpr uint32_t kIdescBMnMajor = 1u << 16;
 
 }  // namespace ptx
