@@ -564,9 +564,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     // everything above overlaps the previous kernel; its outputs (the B operand, the Gram
-    // partials) are read only after this point
-    griddep_wait();
-    griddep_launch_dependents();
+    // partials, the factors) are read only after griddepcontrol.wait.  V is not one of them, so
+    // the producer requests the first stages' V boxes before it waits.
 
     if (warp == 0) {
         if (lane == 0) {
@@ -574,7 +573,26 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             uint32_t phase = 0;
             int armed[kMaxStages];
             for (int s = 0; s < kMaxStages; s++) armed[s] = 0;
-            for (long long b = lo; b < hi; b++) {
+            const int pre = (int)min((long long)p.stages, hi - lo);  // fresh stages: no empty wait
+            for (int i = 0; i < pre; i++) {
+                const long long b = lo + i;
+                const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
+                mbar_arrive_expect_tx(&full[i], stageA + stageB);
+                for (int q = 0; q < p.bps; q++)
+                    tma_load_2d(sA + i * stageA + q * kStageABytes, &tmA, (kb * p.bps + q) * kBlockK, t * kTileM,
+                                &full[i]);
+            }
+            griddep_wait();
+            griddep_launch_dependents();
+            for (int i = 0; i < pre; i++) {
+                const int kb = (int)((lo + i) % p.kblocks);
+                for (int q = 0; q < p.bps; q++)
+                    tma_load_2d(sB + i * stageB + q * boxB, &tmB, (kb * p.bps + q) * kBlockK, 0, &full[i]);
+                armed[i]++;
+            }
+            stage = pre == p.stages ? 0 : pre;
+            phase = pre == p.stages ? 1u : 0u;
+            for (long long b = lo + pre; b < hi; b++) {
                 const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
                 if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty)) break;
                 mbar_arrive_expect_tx(&full[stage], stageA + stageB);
@@ -595,8 +613,13 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 for (int s = 0; s < p.stages; s++)
                     if (armed[s] > 0) mbar_wait_quiet(&full[s], (uint32_t)((armed[s] - 1) & 1));
             }
+        } else {
+            griddep_wait();
+            griddep_launch_dependents();
         }
     } else if (warp == 1) {
+        griddep_wait();
+        griddep_launch_dependents();
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16_f32(kTileM, p.npad);
             int stage = 0, acc = 0;
@@ -642,6 +665,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             mbar_wait_quiet(mdone, 0);
         }
     } else if (warp < 6) {
+        griddep_wait();
+        griddep_launch_dependents();
         // While the first accumulator fills, finish the Gram matrix the update kernel of the
         // previous half-step left as per-CTA partials: this CTA owns entries
         // [c*E/G, (c+1)*E/G); four lanes share an entry and sum the partials in a fixed order.
@@ -711,6 +736,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             b = e;
         }
     } else if constexpr (FNP > 0) {
+        griddep_wait();
+        griddep_launch_dependents();
         fused_prologue<FNP>(p, threadIdx.x - kGemmThreads, sG, sX, sflag);  // warps 6 and 7
     }
     __syncthreads();
