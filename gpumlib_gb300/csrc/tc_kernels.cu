@@ -825,26 +825,45 @@ __global__ void __launch_bounds__(kQThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    // the factors are read only after the kernel that wrote them has completed
-    griddep_wait();
-    griddep_launch_dependents();
+    // the factors are read only after the kernel that wrote them has completed (griddepcontrol.wait);
+    // V is not written by it, so the producer requests the first stages' V tiles before it waits
 
     if (warp == 0) {
         if (lane == 0) {
             int st = 0;
             uint32_t ph = 0;
             int armed[4] = {0, 0, 0, 0};
-            for (int t = blockIdx.x; t < T; t += gridDim.x) {
+            auto load_v = [&](int t, int s2) {  // V' tile: rows i, 64 columns u per box
                 const int ti = t / p.tiles_u, tu = t % p.tiles_u;
+                for (int q = 0; q < 2; q++)
+                    tma_load_2d(const_cast<__nv_bfloat16 *>(sV(s2)) + q * (kQTile * 64), &tmV, tu * kQTile + q * 64,
+                                ti * kQTile, &full[s2]);
+            };
+            auto load_ab = [&](int t, int s2) {
+                const int ti = t / p.tiles_u, tu = t % p.tiles_u;
+                for (int q = 0; q < 2; q++) {
+                    tma_load_2d(sA(s2) + q * boxBytes, &tmA, ti * kQTile + q * 64, 0, &full[s2]);
+                    tma_load_2d(sB(s2) + q * boxBytes, &tmB, tu * kQTile + q * 64, 0, &full[s2]);
+                }
+            };
+            int pre = 0;  // fresh stages: no empty wait
+            for (int t = blockIdx.x; t < T && pre < p.stages; t += gridDim.x, pre++) {
+                mbar_arrive_expect_tx(&full[pre], (uint32_t)stageBytes);
+                load_v(t, pre);
+            }
+            griddep_wait();
+            griddep_launch_dependents();
+            for (int k = 0; k < pre; k++) {
+                load_ab(blockIdx.x + k * gridDim.x, k);
+                armed[k]++;
+            }
+            st = pre == p.stages ? 0 : pre;
+            ph = pre == p.stages ? 1u : 0u;
+            for (int t = blockIdx.x + pre * gridDim.x; t < T; t += gridDim.x) {
                 if (!mbar_wait(&empty[st], ph ^ 1, p.err, kErrWaitEmpty)) break;
                 mbar_arrive_expect_tx(&full[st], (uint32_t)stageBytes);
-                for (int q = 0; q < 2; q++) {
-                    tma_load_2d(sA(st) + q * boxBytes, &tmA, ti * kQTile + q * 64, 0, &full[st]);
-                    tma_load_2d(sB(st) + q * boxBytes, &tmB, tu * kQTile + q * 64, 0, &full[st]);
-                }
-                for (int q = 0; q < 2; q++)  // V' tile: rows i, 64 columns u per box
-                    tma_load_2d(const_cast<__nv_bfloat16 *>(sV(st)) + q * (kQTile * 64), &tmV, tu * kQTile + q * 64,
-                                ti * kQTile, &full[st]);
+                load_ab(t, st);
+                load_v(t, st);
                 armed[st]++;
                 if (++st == p.stages) {
                     st = 0;
@@ -854,8 +873,13 @@ __global__ void __launch_bounds__(kQThreads, 1)
             if (*((volatile int *)p.err) != 0)
                 for (int k = 0; k < p.stages; k++)
                     if (armed[k] > 0) mbar_wait_quiet(&full[k], (uint32_t)((armed[k] - 1) & 1));
+        } else {
+            griddep_wait();
+            griddep_launch_dependents();
         }
     } else if (warp == 1) {
+        griddep_wait();
+        griddep_launch_dependents();
         if (lane == 0) {
             // both operands MN-major: a K16 step is 16 rows of 128 bytes; the second 64-wide box of M / N
             // is boxBytes further (leading byte offset), 8-row groups 1024 bytes apart
@@ -885,6 +909,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
             mbar_wait_quiet(mdone, 0);
         }
     } else {
+        griddep_wait();
+        griddep_launch_dependents();
         const int quarter = warp & 3;          // TMEM lanes this warp may read
         const int c0 = ((warp - 2) >> 2) * 32; // its 32 columns of the tile
         const int i = quarter * 32 + lane;     // this thread's row of the tile (its TMEM lane)
@@ -1394,8 +1420,9 @@ __global__ void __launch_bounds__(kKlThreads)
     // TMEM columns: the numerator accumulator [0, npad), A1 (the tile's factor rows, BF16 pairs)
     // [npad, npad + 64), then nb S/R buffers of 128
     const uint32_t tD2 = tmem, tA1 = tmem + (uint32_t)NP, tD1 = tmem + (uint32_t)(NP + 64);
-    griddep_wait();
-    griddep_launch_dependents();
+    // the previous kernel's outputs (the factor copies, the denominators' partials) are read only
+    // after griddepcontrol.wait; V is not one of them, so the producer requests the first V stages
+    // before it waits
 
     if (warp == 0) {
         if (lane == 0) {
@@ -1404,6 +1431,18 @@ __global__ void __launch_bounds__(kKlThreads)
             // the last phase armed on each full barrier (bit set) and its parity, for the drain below
             uint32_t armed_v = 0, par_v = 0, armed_f = 0, par_f = 0;
             bool ok = true;
+            const long long vpre = min((long long)p.sv, hi - lo);  // fresh V stages: no empty wait
+            for (long long bb = lo; bb < lo + vpre; bb++) {
+                const int t = (int)(bb / p.kblocks), k0 = (int)(bb % p.kblocks) * kKlBlockK;
+                mbar_arrive_expect_tx(&vfull[vi], (uint32_t)kKlVBytes);
+                tma_load_2d(sV(vi), &tmV, k0, t * kTileM, &vfull[vi]);
+                tma_load_2d(sV(vi) + kKlVBytes / 2, &tmV, k0 + 64, t * kTileM, &vfull[vi]);
+                armed_v |= 1u << vi;
+                par_v = (par_v & ~(1u << vi)) | (vph << vi);
+                ring_next(vi, vph, p.sv);
+            }
+            griddep_wait();
+            griddep_launch_dependents();
             for (long long b = lo; b < hi && ok;) {
                 const int t = (int)(b / p.kblocks);
                 const long long e = seg_end(b);
@@ -1427,6 +1466,7 @@ __global__ void __launch_bounds__(kKlThreads)
                     armed_f |= 1u << fi;
                     par_f = (par_f & ~(1u << fi)) | (fph << fi);
                     ring_next(fi, fph, p.sf);
+                    if (bb < lo + vpre) continue;  // its V is already on the way
                     if (!mbar_wait_sleep(&vempty[vi], vph ^ 1, p.err, kErrWaitEmpty)) {
                         ok = false;
                         break;
@@ -1447,8 +1487,13 @@ __global__ void __launch_bounds__(kKlThreads)
                 if (armed_f >> s & 1) mbar_wait_quiet(&ffull[s], par_f >> s & 1);
             for (int s = 0; s < p.sv; s++)
                 if (armed_v >> s & 1) mbar_wait_quiet(&vfull[s], par_v >> s & 1);
+        } else {
+            griddep_wait();
+            griddep_launch_dependents();
         }
     } else if (warp == 1) {
+        griddep_wait();
+        griddep_launch_dependents();
         // The whole warp runs the MMA loop (its state is warp-uniform, barrier tests are voted), and
         // one elected lane issues the products and commits: the issue path stays on warp-uniform
         // values instead of a single divergent lane.
@@ -1577,6 +1622,8 @@ __global__ void __launch_bounds__(kKlThreads)
         }
         __syncwarp();
     } else {
+        griddep_wait();
+        griddep_launch_dependents();
         // finish the denominators (column / row sums of the other factor) from the partials: each of
         // this CTA's entries by all 512 epilogue threads (thread et takes partials et, et + 512, ...,
         // then a fixed tree over lanes and warps), so no warp starts the ratios much later than the rest
