@@ -21,6 +21,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -63,15 +64,44 @@ static gpunmf_status check_device() {
     return GPUNMF_OK;
 }
 
+// The library's memory pool of a device (created once): freed blocks stay in it (release threshold
+// at its maximum) and are reused by later jobs; the default pool is left as the application set it.
+static cudaMemPool_t library_pool(int dev) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    static bool tried[64] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    const int k = dev & 63;
+    if (!tried[k]) {
+        tried[k] = true;
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+            unsigned long long thr = ~0ULL;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+            pools[k] = pool;
+        } else {
+            cudaGetLastError();  // no pool: plain allocations
+        }
+    }
+    return pools[k];
+}
+
+static bool stream_ordered(const gpunmf_job *j) { return j->pool || j->async_alloc; }
+
 cudaError_t job_dev_alloc(gpunmf_job *j, void **p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) return cudaSuccess;
+    if (j->pool) return cudaMallocFromPoolAsync(p, bytes, j->pool, j->stream);
     return j->async_alloc ? cudaMallocAsync(p, bytes, j->stream) : cudaMalloc(p, bytes);
 }
 
 void job_dev_free(gpunmf_job *j, void *p) {
     if (!p) return;
-    if (j->async_alloc)
+    if (stream_ordered(j))
         cudaFreeAsync(p, j->stream);
     else
         cudaFree(p);
@@ -79,8 +109,9 @@ void job_dev_free(gpunmf_job *j, void *p) {
 
 cudaError_t job_h2d(gpunmf_job *j, void *dst, const void *src, size_t bytes) {
     if (bytes == 0) return cudaSuccess;
-    return j->async_alloc ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, j->stream)
-                          : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    // from pageable memory the call returns once the source is staged, so the caller may free it
+    return stream_ordered(j) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, j->stream)
+                             : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
 }
 
 template <class T>
@@ -197,6 +228,10 @@ static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int pre
             return GPUNMF_ERR_CUDA;
         }
         j->own_stream = true;
+    }
+    if (!j->async_alloc) {  // a public job: the library's pool (where the device has one)
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) j->pool = library_pool(dev);
     }
     Sizes z = compute_sizes(rule, n, m, r, precision);
     j->s_h = z.s_h; j->s_w = z.s_w; j->s_g = z.s_g;

@@ -52,6 +52,9 @@ struct gpunmf_job {
     // allocation mode: jobs made by the server use the stream-ordered allocator on their
     // stream (no device-wide synchronisation on free) and a pinned block owned by the server
     bool async_alloc = false;
+    // public jobs: device memory stream-ordered from the library's pool, which keeps freed blocks
+    // for the next job (creating a job then makes no driver allocation once the pool has grown)
+    cudaMemPool_t pool = nullptr;
     bool external_pinned = false;
 };
 

@@ -770,6 +770,14 @@ constexpr int kQThreads = 64 + 32 * kQEpiWarps;
 constexpr int kQTile = 128;
 constexpr int kQVBytes = kQTile * kQTile * 2;
 
+// The hardware's approximate base-2 logarithm (lg2.approx.ftz.f32): its argument s + eps is at
+// least eps >= 1e-30 (s >= 0), a normal float, so flushing subnormals changes nothing.
+__device__ __forceinline__ float lg2_approx(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 struct QParams {
     int tiles_i, tiles_u, npad, stages;
     float eps;
@@ -914,7 +922,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
         const int quarter = warp & 3;          // TMEM lanes this warp may read
         const int c0 = ((warp - 2) >> 2) * 32; // its 32 columns of the tile
         const int i = quarter * 32 + lane;     // this thread's row of the tile (its TMEM lane)
-        const float eps = p.eps;
+        // eps > 0 keeps the log finite in zero-padded rows and columns (V = 0 there, so they add 0)
+        const float eps = fmaxf(p.eps, 1e-30f);
         double dlog = 0.0, ds = 0.0;
         int st = 0, acc = 0;
         uint32_t ph = 0, aph = 0;
@@ -949,8 +958,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
                 for (int e = 0; e < 4; e++) {
                     const float2 vv = __bfloat1622float2(h2[e]);
                     const int j = 8 * k + 2 * e;
-                    plog = fmaf(vv.x, __log2f(sv[j] + eps), plog);
-                    plog = fmaf(vv.y, __log2f(sv[j + 1] + eps), plog);
+                    plog = fmaf(vv.x, lg2_approx(sv[j] + eps), plog);
+                    plog = fmaf(vv.y, lg2_approx(sv[j + 1] + eps), plog);
                     ps += sv[j];
                     ps += sv[j + 1];
                 }
@@ -2762,8 +2771,9 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
 
 gpunmf_status tc_check(gpunmf_job *j) {
     if (!j->tc || !j->tc->err) return GPUNMF_OK;
-    int e = 0;
-    GPUNMF_CUDA_TRY(cudaMemcpy(&e, j->tc->err, sizeof(int), cudaMemcpyDeviceToHost));
+    int e = 0;  // read in the job's stream order (its memory may be stream-ordered)
+    GPUNMF_CUDA_TRY(cudaMemcpyAsync(&e, j->tc->err, sizeof(int), cudaMemcpyDeviceToHost, j->stream));
+    GPUNMF_CUDA_TRY(cudaStreamSynchronize(j->stream));
     if (e != 0) {
         set_error("tensor-core kernel gave up waiting (error bits 0x%x)", e);
         return GPUNMF_ERR_TIMEOUT;
