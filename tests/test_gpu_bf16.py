@@ -140,3 +140,34 @@ def test_bf16_quality_tracks_fp32(gpu, rule, shape):
     assert a[0] == b[0] == 1.0 and a[1] == b[1] == 1.0      # no improvement before the third sample
     scale = np.abs(a[2:]).max()
     assert np.abs(a[2:] - b[2:]).max() <= 2e-2 * scale, (a, b)
+
+
+def test_two_jobs_interleaved_match_alone(gpu):
+    """Two BF16 jobs with the fused half-step kernel, each on its own stream, iterated alternately:
+    every launch follows one on the other stream, so the engine orders the two jobs' fused grids
+    (their CTAs wait on one another, so two of them must not share the SMs).  The kernels are
+    deterministic: the results equal those of each job run alone, bit for bit."""
+    shapes = [(1500, 1100, 64), (900, 1700, 32)]
+    data = []
+    for k, (n, m, r) in enumerate(shapes):
+        g = np.random.Generator(np.random.PCG64(40 + k))
+        V = np.asfortranarray(g.random((n, m), dtype=np.float32))
+        W, H = inputs.factors(50 + k, n, m, r)
+        data.append((V, W, H))
+    alone = []
+    for V, W, H in data:
+        with gpu.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=1e-9, precision="bf16") as nmf:
+            for _ in range(12):
+                nmf.DoIteration()
+            alone.append((nmf.GetW(), nmf.GetH(), nmf.QualityImprovement()))
+    jobs = [gpu.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=1e-9, precision="bf16") for V, W, H in data]
+    try:
+        for _ in range(12):
+            for nmf in jobs:
+                nmf.DoIteration()
+        for nmf, (Wa, Ha, qa) in zip(jobs, alone):
+            assert np.array_equal(nmf.GetW(), Wa) and np.array_equal(nmf.GetH(), Ha)
+            assert nmf.QualityImprovement() == qa
+    finally:
+        for nmf in jobs:
+            nmf.close()
