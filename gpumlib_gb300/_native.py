@@ -43,6 +43,7 @@ SIGNATURES = [
     ("gpunmf_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gpunmf_info", ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_float_p]),
     ("gpunmf_footprint_bytes", ctypes.c_size_t, [ctypes.c_int] * 5),
+    ("gpunmf_trim_pool", ctypes.c_int, []),
     ("gpunmf_fill_uniform", None, [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_size_t, ctypes.c_void_p]),
     ("gpunmf_host_alloc", ctypes.c_void_p, [ctypes.c_size_t]),
     ("gpunmf_host_free", None, [ctypes.c_void_p]),

@@ -580,6 +580,14 @@ gpunmf_status gpunmf_create_random(int rule, int n, int m, int r, const float *V
     return gpunmf_create(rule, n, m, r, V, W.data(), H.data(), eps, precision, stream, out);
 }
 
+gpunmf_status gpunmf_trim_pool(void) {
+    int dev = 0;
+    GPUNMF_CUDA_TRY(cudaGetDevice(&dev));
+    cudaMemPool_t pool = library_pool(dev);
+    if (pool) GPUNMF_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+    return GPUNMF_OK;
+}
+
 gpunmf_status gpunmf_destroy(gpunmf_handle h) {
     CHECK_HANDLE(h);
     if (h->stream) cudaStreamSynchronize(h->stream);

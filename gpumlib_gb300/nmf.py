@@ -202,3 +202,8 @@ def footprint_bytes(rule, n, m, r, precision="fp32"):
 
 def device_count():
     return int(_native.load().gpunmf_device_count())
+
+
+def trim_pool():
+    """Hand the library's unused pooled device memory back to the driver (current device)."""
+    _native.check(_native.load().gpunmf_trim_pool())

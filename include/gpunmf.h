@@ -172,6 +172,11 @@ gpunmf_status gpunmf_info(gpunmf_handle h, int *rule, int *n, int *m, int *r,
 /* Device bytes a job of this shape holds (admission accounting). */
 size_t gpunmf_footprint_bytes(int rule, int n, int m, int r, int precision);
 
+/* Jobs made through this API take device memory from a pool the library keeps per device, so
+ * creating a job after another was destroyed needs no driver allocation.  This hands the pool's
+ * unused memory back to the driver (for the current device); jobs still alive keep theirs. */
+gpunmf_status gpunmf_trim_pool(void);
+
 /* Host-only: out[k] = uniform[0,1) value number offset+k of the counter-based
  * generator keyed by seed (the generator gpunmf_create_random uses). */
 void gpunmf_fill_uniform(unsigned long long seed, unsigned long long offset, size_t count, float *out);

@@ -171,3 +171,20 @@ def test_two_jobs_interleaved_match_alone(gpu):
     finally:
         for nmf in jobs:
             nmf.close()
+
+
+def test_pool_reuse_and_trim(gpu):
+    """Jobs take device memory from the library's pool: a job made after another was destroyed reuses
+    it, after trim_pool it is allocated afresh; the results do not depend on either."""
+    n, m, r = 1200, 900, 64
+    V = inputs.uniform_matrix(81, n, m)
+    W, H = inputs.factors(82, n, m, r)
+    outs = []
+    for trim in (False, False, True):
+        if trim:
+            gpu.trim_pool()
+        with gpu.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=1e-9, precision="bf16", quality_interval=0) as nmf:
+            nmf.Iterate(4)
+            outs.append((nmf.GetW(), nmf.GetH()))
+    for Wk, Hk in outs[1:]:
+        assert np.array_equal(Wk, outs[0][0]) and np.array_equal(Hk, outs[0][1])
