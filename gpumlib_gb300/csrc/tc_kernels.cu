@@ -1332,7 +1332,138 @@ struct KlParams {
     const float *sum_partials;  // [count][npad] partial sums of the other factor
     float *sum_out;             // [npad]
     int sum_count;
+    // fused update (X != null): after the stream every CTA updates its slice of the factor's rows,
+    // [c*rows/G, (c+1)*rows/G), from its tiles' partial slots (as the separate update kernel does)
+    float *X;                   // H (r x m, element (a, u) at u*r + a) or W (n x r, (i, a) at a*ldx + i)
+    __nv_bfloat16 *Xb, *Xr;     // BF16 copies: (a, row) at a*ldb + row; (row, a) at row*ldr + a
+    long long ldb, ldr, ldx;
+    int is_w, rows, r, additive;
+    const int *slot_ptr, *slot_list;  // each tile's slots in K order
+    int *tile_cnt, *tile_rd;          // per tile: partial products out, readers done (the last resets)
+    const int *tile_readers;          // per tile: how many CTAs read it
+    int *sum_cnt;                     // [2]: CTAs whose denominator entries are out; CTAs done (last resets)
+    float *sum_part_out;              // [grid][npad] sums of this CTA's new rows (the next kernel's denominators)
 };
+
+constexpr int kKlEpiWarps = 16;  // 4 per TMEM lane quarter, 32 columns of each block each
+constexpr int kKlThreads = 64 + 32 * kKlEpiWarps;  // warp 0 TMA, warp 1 MMA, then the ratio epilogue
+constexpr int kKlTailMaxSlots = 16;  // slots of one tile the fused update stages (checked on the host)
+
+// Fused KL update (all 576 threads, after the stream; the rings' shared memory is free).  For each
+// chunk of up to 128 of this CTA's rows: wait until the chunk's tiles have all their partial
+// products (and, before the first, until every CTA has published its denominator entries), copy the
+// chunk's rows of every slot into shared memory at once (cp.async), sum them in K order, apply
+// X *= num / max(sum, eps) (nmf_kernels.cu:289,337), or X = max(0, X + X / max(sum, eps) (num - sum))
+// for the additive rule (nmf_kernels_additive_divergence.cu:101-104), write X and its two BF16
+// copies, and add the new rows to this CTA's sums, the next kernel's denominators.  The host checks
+// that the staging fits (rows x slots per chunk).
+template <int NP>
+__device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, int *sflag) {
+    constexpr int LD = NP + 1;  // sX[128][NP + 1]
+    const int tid = threadIdx.x, c = blockIdx.x, G = gridDim.x;
+    const int rows = p.rows, r = p.r;
+    const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
+    float *sX = smem;
+    float *sSum = sX + 128 * LD, *sRaw = sSum + NP;
+    float *sP = sRaw + NP;  // staged slot rows: [part][slot][row][NP]
+    float colsum = 0.f;     // thread a < NP: this CTA's sum of the new X(., a)
+    bool first = true;
+    for (long long xb = x0; xb < x1; xb += 128) {
+        const int nr = (int)min(128LL, x1 - xb);
+        const int t0 = (int)(xb / kTileM), t1 = (int)((xb + nr - 1) / kTileM);  // t1 <= t0 + 1
+        const int split = (int)min((long long)nr, (long long)(t0 + 1) * kTileM - xb);  // rows in t0
+        if (tid == 0) {
+            bool ok = !first || flag_wait_ge(p.sum_cnt, G, p.err, kErrWaitTile);
+            for (int t = t0; t <= t1 && ok; t++)
+                ok = flag_wait_ge(p.tile_cnt + t, p.slot_ptr[t + 1] - p.slot_ptr[t], p.err, kErrWaitTile);
+            sflag[0] = ok ? 1 : 0;
+        }
+        __syncthreads();
+        if (!sflag[0]) return;  // uniform; the error word is set
+        __threadfence();
+        // stage: part k covers chunk rows [k ? split : 0, k ? nr : split) of tile t0 + k
+        const int ns0 = p.slot_ptr[t0 + 1] - p.slot_ptr[t0];
+        const int ns1 = t1 > t0 ? p.slot_ptr[t1 + 1] - p.slot_ptr[t1] : 0;
+        const int n0 = split, n1 = nr - split;
+        const int lr0 = (int)(xb - (long long)t0 * kTileM);  // first chunk row's row in tile t0
+        float *sP1 = sP + (size_t)ns0 * n0 * NP;
+        {
+            const int q4 = NP / 4, per0 = ns0 * n0 * q4, total = per0 + ns1 * n1 * q4;
+            for (int k = tid; k < total; k += kKlThreads) {
+                int part = k >= per0, kk = part ? k - per0 : k;
+                const int nrows = part ? n1 : n0;
+                const int q = kk / (nrows * q4), rem = kk - q * nrows * q4;
+                const int rho = rem / q4, a4 = rem - rho * q4;
+                const int t = t0 + part, lr = part ? rho : lr0 + rho;
+                const int slot = p.slot_list[p.slot_ptr[t] + q];
+                const float *src = p.partials + ((size_t)slot * kTileM + lr) * NP + 4 * a4;
+                float *dst = (part ? sP1 : sP) + ((size_t)q * nrows + rho) * NP + 4 * a4;
+                cp_async16(dst, src, true);
+            }
+            cp_async_commit();
+        }
+        if (first) {
+            for (int a = tid; a < NP; a += kKlThreads) {
+                const float sraw = __ldcg(p.sum_out + a);
+                sRaw[a] = sraw;
+                sSum[a] = fmaxf(sraw, p.eps);
+            }
+            first = false;
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        // numerators (slots in K order) and the update
+        for (int e = tid; e < nr * NP; e += kKlThreads) {
+            const int rho = e / NP, a = e - rho * NP;
+            const int part = rho >= split, prow = part ? rho - split : rho;
+            const int ns = part ? ns1 : ns0, nrows = part ? n1 : n0;
+            const float *base = (part ? sP1 : sP) + (size_t)prow * NP + a;
+            float num = 0.f;
+            for (int q = 0; q < ns; q++) num += base[(size_t)q * nrows * NP];
+            float xn = 0.f;
+            if (a < r) {
+                const long long grow = xb + rho;
+                const long long xi = p.is_w ? (long long)a * p.ldx + grow : grow * r + a;
+                const float x = p.X[xi];
+                if (p.additive) {
+                    xn = x + (x / sSum[a]) * (num - sRaw[a]);
+                    xn = xn < 0.f ? 0.f : xn;
+                } else {
+                    xn = x * (num / sSum[a]);
+                }
+                p.X[xi] = xn;
+            }
+            sX[rho * LD + a] = xn;
+        }
+        __syncthreads();
+        if (tid == 0)
+            for (int t = t0; t <= t1; t++)
+                if (atomicAdd(p.tile_rd + t, 1) == p.tile_readers[t] - 1) {  // the last reader resets
+                    p.tile_cnt[t] = 0;
+                    p.tile_rd[t] = 0;
+                }
+        // the BF16 copies: Xb (a, row) rows fastest; Xr (row, a) a fastest, zero beyond r
+        for (int e = tid; e < r * nr; e += kKlThreads) {
+            const int a = e / nr, rho = e - a * nr;
+            p.Xb[(long long)a * p.ldb + xb + rho] = __float2bfloat16_rn(sX[rho * LD + a]);
+        }
+        for (int e = tid; e < nr * NP; e += kKlThreads) {
+            const int rho = e / NP, a = e - rho * NP;
+            p.Xr[(xb + rho) * p.ldr + a] = __float2bfloat16_rn(sX[rho * LD + a]);
+        }
+        if (tid < NP)
+            for (int rho = 0; rho < nr; rho++) colsum += sX[rho * LD + tid];
+        __syncthreads();
+    }
+    if (tid < NP) p.sum_part_out[(size_t)c * NP + tid] = colsum;
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(p.sum_cnt + 1, 1) == G - 1) {  // every CTA is past its waits: reset
+            p.sum_cnt[1] = 0;
+            atomicExch(p.sum_cnt, 0);
+        }
+    }
+}
 
 constexpr int kKlBlockK = 128;            // K columns per block
 constexpr int kKlVBytes = kTileM * kKlBlockK * 2;  // 32 KB: two 64-column boxes
@@ -1352,6 +1483,18 @@ __device__ __forceinline__ uint32_t sw128(int row, int chunk) {
     return (uint32_t)(row * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
+// barrier of the 16 KL epilogue warps that ORs a per-thread flag (the same answer in every thread)
+__device__ __forceinline__ bool kl_epi_bar_or(bool v) {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 3, 512, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((unsigned)v)
+        : "memory");
+    return r != 0;
+}
+
 // one lane of the (fully active) warp, the same every call
 __device__ __forceinline__ bool elect_one() {
     uint32_t pred = 0;
@@ -1366,8 +1509,6 @@ __device__ __forceinline__ void ring_next(int &i, uint32_t &ph, int n) {
     }
 }
 
-constexpr int kKlEpiWarps = 16;  // 4 per TMEM lane quarter, 32 columns of each block each
-constexpr int kKlThreads = 64 + 32 * kKlEpiWarps;  // warp 0 TMA, warp 1 MMA, then the ratio epilogue
 
 // NK = npad / 16: the K16 steps of MMA1 (compile-time, so the MMA thread issues straight-line code)
 template <int NK>
@@ -1663,6 +1804,10 @@ __global__ void __launch_bounds__(kKlThreads)
                 asm volatile("bar.sync 3, 512;" ::: "memory");
             }
         }
+        if (p.X && threadIdx.x == 64) {  // this CTA's denominator entries are out (the fused tails wait)
+            __threadfence();
+            atomicAdd(p.sum_cnt, 1);
+        }
         const int quarter = warp & 3;     // TMEM lanes this warp may access
         const int part = (warp - 2) >> 2;  // which 32 of the block's 128 columns; also its share of the D2 drain
         const float eps_pos = fmaxf(p.eps, 1e-30f);
@@ -1723,8 +1868,9 @@ __global__ void __launch_bounds__(kKlThreads)
                 ring_next(vi, vph, p.sv);
                 ring_next(di, dph, p.nb);
             }
-            if (!ok) break;
-            if (!mbar_wait_sleep(tfull, (uint32_t)(seg & 1), p.err, kErrWaitTmemFull)) break;
+            // the 16 warps leave together (the drain below ends at a barrier of all of them)
+            if (kl_epi_bar_or(!ok)) break;
+            if (kl_epi_bar_or(!mbar_wait_sleep(tfull, (uint32_t)(seg & 1), p.err, kErrWaitTmemFull))) break;
             tc_fence_after();
             float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
             for (int c = part * 16; c < NP; c += 64) {  // the four warps of a quarter take turns by 16 columns
@@ -1740,6 +1886,11 @@ __global__ void __launch_bounds__(kKlThreads)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(tempty);
+            if (p.X) {  // this segment's partial product is out: count it on its tile
+                __threadfence();
+                asm volatile("bar.sync 3, 512;" ::: "memory");
+                if (threadIdx.x == 64) atomicAdd(&p.tile_cnt[b / p.kblocks], 1);
+            }
             seg++;
             b = e;
         }
@@ -1749,6 +1900,8 @@ __global__ void __launch_bounds__(kKlThreads)
         tc_fence_after();
         tmem_dealloc(tmem, 512);
     }
+    if (p.X && __syncthreads_and(*((volatile int *)p.err) == 0))
+        kl_fused_tail<NP>(p, reinterpret_cast<float *>(base), reinterpret_cast<int *>(red + 16));
 }
 
 // KL update (nmf_kernels.cu:289,337 with the eps clamp of :104,190): X *= num / max(sum, eps)
@@ -1897,6 +2050,10 @@ struct KlGemm {
     gpunmf::KlParams p;
     int grid = 0, smem = 0;
     int *slot_ptr = nullptr, *slot_list = nullptr, *tile_slots = nullptr;
+    // fused update: whether it fits, its counters and the per-CTA sums of the new rows
+    bool fusable = false;
+    int *counters = nullptr;   // [tiles] arrivals, [tiles] readers done, [tiles] readers, [2] sums
+    float *row_sums = nullptr; // [grid][npad]
 };
 
 struct TcState {
@@ -2241,6 +2398,65 @@ static cudaError_t set_kl_smem_once() {
     return result;
 }
 
+// The stream of the last launch per device of a grid whose CTAs wait on one another (see
+// launch_resident); a job that is torn down (its stream drained first) forgets its stream here.
+struct LastFused {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    bool used = false;
+    cudaEvent_t ev = nullptr;
+};
+static LastFused g_last_fused[64];
+
+static void forget_fused_stream(cudaStream_t s) {
+    for (LastFused &L : g_last_fused) {
+        std::lock_guard<std::mutex> lock(L.mu);
+        if (L.used && L.stream == s) L.used = false;
+    }
+}
+
+// Launch of a grid whose CTAs wait on one another (every wait bounded): the grid (at most one CTA
+// per SM) must be resident at once.  On one stream that holds: the previous kernel's CTAs never wait
+// on the next one.  Two such grids on different streams could each hold part of the SMs and wait for
+// the rest, so:
+//  - a launch being captured into a graph (the server's iteration chunks, replayed on many streams)
+//    is cooperative, which makes the residency of its grid a launch condition;
+//  - otherwise these launches of this process are serialised across streams (a launch on a stream
+//    other than the last one's first waits for everything submitted to that stream), which keeps the
+//    programmatic dependent launch that a cooperative launch forgoes (~6% per iteration).
+// at[0] holds the programmatic-serialisation attribute on entry; launch() launches with cfg.
+template <class Launch>
+static cudaError_t launch_resident(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, Launch launch) {
+    const cudaStream_t s = cfg.stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) return e;
+    if (cap != cudaStreamCaptureStatusNone) {
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.numAttrs = 1;
+        return launch();
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    LastFused &L = g_last_fused[dev & 63];
+    std::lock_guard<std::mutex> lock(L.mu);
+    cudaStreamCaptureStatus lcap = cudaStreamCaptureStatusNone;
+    if (L.used && L.stream != s && cudaStreamIsCapturing(L.stream, &lcap) == cudaSuccess &&
+        lcap == cudaStreamCaptureStatusNone) {  // (work being captured there is not running yet)
+        if (!L.ev) {
+            e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
+        e = cudaEventRecord(L.ev, L.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, L.ev, 0);
+        if (e != cudaSuccess) return e;
+    }
+    L.stream = s;
+    L.used = true;
+    return launch();
+}
+
 static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npad, float **partials, int *err) {
     const int tiles = ceil_div(rows, kTileM);
     const int kblocks = ceil_div(K, kKlBlockK);
@@ -2299,7 +2515,56 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
         return GPUNMF_ERR_NOMEM;
     }
     g.p.partials = *partials;
+    // the fused update's staging (shared memory of the rings, free after the stream): per chunk of up
+    // to 128 rows, the chunk's rows of every slot of its one or two tiles, next to the new rows
+    {
+        const int G = g.grid;
+        const size_t room = (size_t)sv * kKlVBytes + (size_t)sf * fbytes;
+        const size_t fixed_tail = ((size_t)128 * (npad + 1) + 2 * npad) * sizeof(float);
+        std::vector<int> readers(tiles, 0);
+        bool fits = true;
+        for (int c = 0; c < G && fits; c++) {
+            const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
+            for (long long xb = x0; xb < x1; xb += 128) {
+                const long long nr = std::min(128LL, x1 - xb);
+                const int t0 = (int)(xb / kTileM), t1 = (int)((xb + nr - 1) / kTileM);
+                const long long split = std::min(nr, (long long)(t0 + 1) * kTileM - xb);
+                const long long ns0 = ptr[t0 + 1] - ptr[t0], ns1 = t1 > t0 ? ptr[t1 + 1] - ptr[t1] : 0;
+                const size_t staged = (size_t)(ns0 * split + ns1 * (nr - split)) * npad * sizeof(float);
+                if (fixed_tail + staged > room) fits = false;
+                for (int t = t0; t <= t1; t++) readers[t]++;
+            }
+        }
+        if (fits) {
+            const size_t nc = (size_t)3 * tiles + 2;
+            e = job_dev_alloc(j, (void **)&g.counters, nc * sizeof(int));
+            if (e == cudaSuccess) e = cudaMemsetAsync(g.counters, 0, nc * sizeof(int), j->stream);
+            if (e == cudaSuccess) e = job_h2d(j, g.counters + 2 * tiles, readers.data(), tiles * sizeof(int));
+            if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&g.row_sums, (size_t)G * npad * sizeof(float));
+            if (e != cudaSuccess) {
+                set_error("KL fused-update workspace allocation failed: %s", cudaGetErrorString(e));
+                cudaGetLastError();
+                return GPUNMF_ERR_NOMEM;
+            }
+            g.fusable = true;
+        }
+    }
     return GPUNMF_OK;
+}
+
+// Per-CTA sums over a factor's rows, in the row partition of the fused update with G CTAs
+// (out[c][a] = sum over rows [c*rows/G, (c+1)*rows/G) of X(row, a), in row order; 0 for a >= r):
+// the denominators' partials of the first kernel, before any fused update has left them.
+__global__ void kl_row_sums_kernel(const float *__restrict__ X, int is_w, long long ldx, int rows, int r,
+                                   int npad, float *__restrict__ out) {
+    const int c = blockIdx.x, G = gridDim.x;
+    const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
+    for (int a = threadIdx.x; a < npad; a += blockDim.x) {
+        float s = 0.f;
+        if (a < r)
+            for (long long x = x0; x < x1; x++) s += is_w ? X[(long long)a * ldx + x] : X[x * r + a];
+        out[(size_t)c * npad + a] = s;
+    }
 }
 
 static cudaError_t launch_kl_gemm(KlGemm &g, cudaStream_t s) {
@@ -2313,13 +2578,17 @@ static cudaError_t launch_kl_gemm(KlGemm &g, cudaStream_t s) {
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    switch (g.p.npad / 16) {
+    auto launch = [&]() -> cudaError_t {
+        switch (g.p.npad / 16) {
 #define KLCASE(NK) \
     case NK: return cudaLaunchKernelEx(&cfg, tc_kl_gemm_kernel<NK>, g.tmV, g.tmA1, g.tmF, g.p);
-        KLCASE(1) KLCASE(2) KLCASE(3) KLCASE(4) KLCASE(5) KLCASE(6) KLCASE(7) KLCASE(8)
+            KLCASE(1) KLCASE(2) KLCASE(3) KLCASE(4) KLCASE(5) KLCASE(6) KLCASE(7) KLCASE(8)
 #undef KLCASE
-    }
-    return cudaErrorInvalidValue;
+        }
+        return cudaErrorInvalidValue;
+    };
+    // with the update fused its CTAs wait on one another (tile arrivals, the denominators)
+    return g.p.X ? launch_resident(cfg, at, launch) : launch();
 }
 
 static cudaError_t launch_kl_update(const KlUpdParams &u, int rp, bool is_w, cudaStream_t s) {
@@ -2397,6 +2666,25 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
     if (st != GPUNMF_OK) return st;
     t->kh.p.sum_partials = t->SP_w; t->kh.p.sum_out = t->S_w; t->kh.p.sum_count = cw;
     t->kw.p.sum_partials = t->SP_h; t->kw.p.sum_out = t->S_h; t->kw.p.sum_count = ch;
+    if (t->kh.fusable && t->kw.fusable) {
+        // each half-step updates its factor in its own tail: the H-step's rows are the columns u of
+        // H, the W-step's the rows i of W; each leaves per-CTA sums of its new rows, which the other
+        // half-step's kernel finishes into its denominators
+        auto fuse = [&](KlGemm &g, float *X, __nv_bfloat16 *Xb, long long ldb, __nv_bfloat16 *Xr, long long ldx,
+                        int is_w, int rows, const KlGemm &other) {
+            const int tiles = g.p.tiles;
+            g.p.X = X; g.p.Xb = Xb; g.p.ldb = ldb; g.p.Xr = Xr; g.p.ldr = t->ldr; g.p.ldx = ldx;
+            g.p.is_w = is_w; g.p.rows = rows; g.p.r = r; g.p.additive = rule_is_additive(j->rule) ? 1 : 0;
+            g.p.slot_ptr = g.slot_ptr; g.p.slot_list = g.slot_list;
+            g.p.tile_cnt = g.counters; g.p.tile_rd = g.counters + tiles; g.p.tile_readers = g.counters + 2 * tiles;
+            g.p.sum_cnt = g.counters + 3 * tiles;
+            g.p.sum_part_out = g.row_sums;
+            g.p.sum_partials = other.row_sums;
+            g.p.sum_count = other.grid;
+        };
+        fuse(t->kh, j->H, t->Hb, t->ldh, t->Hc, 0, 0, m, t->kw);
+        fuse(t->kw, j->W, t->Wb, t->ldw, t->Wr, n, 1, n, t->kh);
+    }
     // H-step: rows u; V tile from Vb, A1 = Hc rows u, F = Wr rows i
     st = make_map(&t->kh.tmV, t->Vb, n, m, t->ldv, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->kh.tmA1, t->Hc, r, m, t->ldr, kTileM);
@@ -2606,8 +2894,14 @@ gpunmf_status tc_prepare(gpunmf_job *j) {
         convert_rowmajor_kernel<<<std::min(1024, ceil_div((long long)j->m * t->ldr, 256)), 256, 0, s>>>(
             j->H, j->m, j->r, 0, false, t->Hc, t->ldr);
         GPUNMF_CUDA_TRY(cudaGetLastError());
-        // column sums of the initial W, finished by the first H-step kernel
-        GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 0), t->npad, true, s));
+        // column sums of the initial W, finished by the first H-step kernel: in the fused W-step's row
+        // partition where the updates are fused, else as the update kernel leaves them
+        if (t->kh.p.X) {
+            kl_row_sums_kernel<<<t->kw.grid, 128, 0, s>>>(j->W, 1, j->n, j->n, j->r, t->npad, t->kw.row_sums);
+            GPUNMF_CUDA_TRY(cudaGetLastError());
+        } else {
+            GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 0), t->npad, true, s));
+        }
         return GPUNMF_OK;
     }
     if (t->gh.fnp) {
@@ -2645,23 +2939,6 @@ static cudaError_t launch_gemm_cfg(TcGemm &g, cudaLaunchConfig_t &cfg) {
     }
 }
 
-// The stream of the last fused-update launch per device (see launch_gemm); a job that is torn down
-// (its stream drained first) forgets its stream here.
-struct LastFused {
-    std::mutex mu;
-    cudaStream_t stream = nullptr;
-    bool used = false;
-    cudaEvent_t ev = nullptr;
-};
-static LastFused g_last_fused[64];
-
-static void forget_fused_stream(cudaStream_t s) {
-    for (LastFused &L : g_last_fused) {
-        std::lock_guard<std::mutex> lock(L.mu);
-        if (L.used && L.stream == s) L.used = false;
-    }
-}
-
 static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.grid);
@@ -2674,42 +2951,7 @@ static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     if (!g.fnp) return launch_gemm_cfg(g, cfg);
-    // The fused update's CTAs wait on one another (tile arrivals, the Gram assembly; every wait is
-    // bounded), so its grid (at most one CTA per SM) must be resident at once.  On one stream that
-    // holds: the previous kernel's CTAs never wait on the next one.  Two fused grids on different
-    // streams could each hold part of the SMs and wait for the rest, so:
-    //  - a launch being captured into a graph (the server's iteration chunks, replayed on many
-    //    streams) is cooperative, which makes the residency of its grid a launch condition;
-    //  - otherwise fused launches of this process are serialised across streams (a launch on a
-    //    stream other than the last one's first waits for everything submitted to that stream),
-    //    which keeps the programmatic dependent launch that a cooperative launch forgoes (~6% per
-    //    iteration).
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    cudaError_t e = cudaStreamIsCapturing(s, &cap);
-    if (e != cudaSuccess) return e;
-    if (cap != cudaStreamCaptureStatusNone) {
-        at[0].id = cudaLaunchAttributeCooperative;
-        at[0].val.cooperative = 1;
-        return launch_gemm_cfg(g, cfg);
-    }
-    int dev = 0;
-    cudaGetDevice(&dev);
-    LastFused &L = g_last_fused[dev & 63];
-    std::lock_guard<std::mutex> lock(L.mu);
-    cudaStreamCaptureStatus lcap = cudaStreamCaptureStatusNone;
-    if (L.used && L.stream != s && cudaStreamIsCapturing(L.stream, &lcap) == cudaSuccess &&
-        lcap == cudaStreamCaptureStatusNone) {  // (work being captured there is not running yet)
-        if (!L.ev) {
-            e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
-            if (e != cudaSuccess) return e;
-        }
-        e = cudaEventRecord(L.ev, L.stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, L.ev, 0);
-        if (e != cudaSuccess) return e;
-    }
-    L.stream = s;
-    L.used = true;
-    return launch_gemm_cfg(g, cfg);
+    return launch_resident(cfg, at, [&] { return launch_gemm_cfg(g, cfg); });
 }
 
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
@@ -2722,18 +2964,20 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
     if (rule_is_kl(j->rule)) {
         // H <- H .* [W'(V ./ (WH + eps))] ./ max(colsum W, eps); the kernel also finishes colsum W
         // (additive KL: the same numerator, applied as H + (H / max(colsum W, eps)) (num - colsum W))
+        // (one launch per half-step where the update is fused into the product kernel's tail)
+        const bool fused = t->kh.p.X != nullptr;
         mark_begin(j);
         GPUNMF_CUDA_TRY(launch_kl_gemm(t->kh, s));
         mark_end(j);
-        GPUNMF_CUDA_TRY(launch_kl_update(kl_params_h(j, 1), t->npad, false, s));
-        j->launches += 2;
+        if (!fused) GPUNMF_CUDA_TRY(launch_kl_update(kl_params_h(j, 1), t->npad, false, s));
+        j->launches += fused ? 1 : 2;
         if (!updateW) return GPUNMF_OK;
         // W <- W .* [(V ./ (WH + eps)) H'] ./ max(rowsum H, eps) with the new H
         mark_begin(j);
         GPUNMF_CUDA_TRY(launch_kl_gemm(t->kw, s));
         mark_end(j);
-        GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 1), t->npad, true, s));
-        j->launches += 2;
+        if (!fused) GPUNMF_CUDA_TRY(launch_kl_update(kl_params_w(j, 1), t->npad, true, s));
+        j->launches += fused ? 1 : 2;
         return GPUNMF_OK;
     }
     if (t->gh.fnp) {
@@ -2784,11 +3028,12 @@ gpunmf_status tc_check(gpunmf_job *j) {
 void tc_destroy(gpunmf_job *j) {
     TcState *t = j->tc;
     if (!t) return;
-    if (t->gh.fnp) forget_fused_stream(j->stream);
+    forget_fused_stream(j->stream);
     void *ptrs[] = {t->Vb, t->Vbt, t->Wb, t->Hb, t->P_h, t->P_w, t->err, t->G_h, t->G_w, t->GP_h, t->GP_w,
                     t->gh.slot_ptr, t->gh.slot_list, t->gw.slot_ptr, t->gw.slot_list,
                     t->gh.tile_slots, t->gw.tile_slots, t->Wr, t->Hc, t->S_w, t->S_h, t->SP_w, t->SP_h,
                     t->kh.slot_ptr, t->kh.slot_list, t->kh.tile_slots, t->kw.slot_ptr, t->kw.slot_list,
+                    t->kh.counters, t->kh.row_sums, t->kw.counters, t->kw.row_sums,
                     t->kw.tile_slots, t->gh.counters, t->gh.grams, t->gw.counters, t->gw.grams};
     for (void *p : ptrs) job_dev_free(j, p);
     delete t;
