@@ -1347,7 +1347,6 @@ struct KlParams {
 
 constexpr int kKlEpiWarps = 16;  // 4 per TMEM lane quarter, 32 columns of each block each
 constexpr int kKlThreads = 64 + 32 * kKlEpiWarps;  // warp 0 TMA, warp 1 MMA, then the ratio epilogue
-constexpr int kKlTailMaxSlots = 16;  // slots of one tile the fused update stages (checked on the host)
 
 // Fused KL update (all 576 threads, after the stream; the rings' shared memory is free).  For each
 // chunk of up to 128 of this CTA's rows: wait until the chunk's tiles have all their partial
