@@ -135,6 +135,21 @@ struct FusedLayout {
 
 __device__ __forceinline__ void wk_bar() { asm volatile("bar.sync 2, 64;" ::: "memory"); }
 
+// N consecutive floats from shared memory, N * 4-byte aligned (N = 4: one 16-byte load)
+template <int N>
+__device__ __forceinline__ void lds_vec(const float *src, float (&v)[N]) {
+    if constexpr (N == 4) {
+        const float4 t = *reinterpret_cast<const float4 *>(src);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (N == 2) {
+        const float2 t = *reinterpret_cast<const float2 *>(src);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) v[i] = src[i];
+    }
+}
+
 // rows [row0, row0 + nrows) (nrows <= 64) of a factor into sX[rho][a], zero elsewhere, up to 32
 // loads in flight per thread.  w_layout: W(i, a) at a*ld + i (threads along i); else H(a, u) at
 // u*r + a (threads along a).
@@ -295,10 +310,9 @@ __device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float
         wk_bar();
     }
     cp_async_wait_all();
-    __threadfence();
-    wk_bar();
+    wk_bar();  // the slice's Gram entries are written by both warps: one release publishes them
     if (wt == 0) {
-        atomicAdd(pr.red_cnt, 1);
+        red_release_add(pr.red_cnt, 1);
         sflag[2] = flag_wait_ge(pr.red_cnt, G, pr.err, kErrWaitGram) ? 1 : 0;
     }
     wk_bar();
@@ -307,11 +321,14 @@ __device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float
     cp_async_commit();
     cp_async_wait_all();
     wk_bar();
-    if (wt == 0 && atomicAdd(pr.red_cnt + 1, 1) == G - 1) {  // every CTA is past the wait: reset
+    // count this CTA past the wait; the answer is used after the denominators (the atomic's round
+    // trip overlaps them): the last CTA resets both counters
+    const int passed = wt == 0 ? atomicAdd(pr.red_cnt + 1, 1) : 0;
+    chunk_denominators<NP, 64>(sX, sG, wt, wk_bar);
+    if (wt == 0 && passed == G - 1) {
         pr.red_cnt[1] = 0;
         atomicExch(pr.red_cnt, 0);
     }
-    chunk_denominators<NP, 64>(sX, sG, wt, wk_bar);
 }
 
 // Tail of the fused update (all 256 threads, after the GEMM): per chunk of this CTA's rows, wait
@@ -368,9 +385,8 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             sSl[tid * (kFusedSlots + 1)] = ns;
             for (int q = 0; q < ns; q++) sSl[tid * (kFusedSlots + 1) + 1 + q] = pr.slot_list[q0 + q];
         }
-        __syncthreads();
+        __syncthreads();      // thread 0's acquire loads and this barrier order the slot reads below
         if (!*sflag) return;  // uniform
-        __threadfence();
         float num[L::RPT][L::APT];
 #pragma unroll
         for (int k = 0; k < L::RPT; k++)
@@ -431,12 +447,13 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
                 num[k][q] = v;
             }
         __syncthreads();  // old rows and partial slots read by every thread
-        if (tid == 0)
-            for (int t = t0; t <= t1; t++)
-                if (atomicAdd(pr.tile_rd + t, 1) == pr.tile_readers[t] - 1) {  // the last reader resets
-                    pr.tile_cnt[t] = 0;
-                    pr.tile_rd[t] = 0;
-                }
+        // count this CTA as a reader of the chunk's tiles; the answers are used at the end of the
+        // chunk (the round trip overlaps the writes): the last reader of a tile resets its counters
+        int rd0 = 0, rd1 = 0;
+        if (tid == 0) {
+            rd0 = atomicAdd(pr.tile_rd + t0, 1);
+            if (t1 > t0) rd1 = atomicAdd(pr.tile_rd + t1, 1);
+        }
 #pragma unroll
         for (int k = 0; k < L::RPT; k++)
 #pragma unroll
@@ -465,15 +482,22 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
 #pragma unroll 2
         for (int rr = 0; rr < nr; rr++) {
             float xa[GB], xb2[GB];
-#pragma unroll
-            for (int i = 0; i < GB; i++) {
-                xa[i] = sX[rr * L::LDX + ga0 + i];
-                xb2[i] = sX[rr * L::LDX + gb0 + i];
-            }
+            lds_vec<GB>(sX + rr * L::LDX + ga0, xa);
+            lds_vec<GB>(sX + rr * L::LDX + gb0, xb2);
 #pragma unroll
             for (int i = 0; i < GB; i++)
 #pragma unroll
                 for (int k = 0; k < GB; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
+        }
+        if (tid == 0) {
+            if (rd0 == pr.tile_readers[t0] - 1) {
+                pr.tile_cnt[t0] = 0;
+                pr.tile_rd[t0] = 0;
+            }
+            if (t1 > t0 && rd1 == pr.tile_readers[t1] - 1) {
+                pr.tile_cnt[t1] = 0;
+                pr.tile_rd[t1] = 0;
+            }
         }
     }
 #pragma unroll
@@ -727,10 +751,10 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 aphase ^= 1;
             }
             if constexpr (FNP > 0) {
-                // this segment's partial product is out: count it on its tile
-                __threadfence();
+                // this segment's partial product is out: count it on its tile (the four warps'
+                // stores are ordered before the barrier, one release publishes them)
                 epi_bar();
-                if (threadIdx.x == 64) atomicAdd(&p.tile_cnt[t], 1);
+                if (threadIdx.x == 64) red_release_add(&p.tile_cnt[t], 1);
             }
             seg++;
             b = e;
@@ -999,14 +1023,13 @@ __global__ void __launch_bounds__(kQThreads, 1)
             sm += red[kQEpiWarps + w];
         }
         p.partial[blockIdx.x] = 0.30102999566398120 * l - sm;  // log10(x) = log2(x) log10(2)
-        __threadfence();
-        reinterpret_cast<volatile int *>(red)[0] = atomicAdd(p.done, 1) == (int)gridDim.x - 1;
+        // publishes this partial; the last CTA's add also acquires every other CTA's
+        reinterpret_cast<volatile int *>(red)[0] = atom_acq_rel_add(p.done, 1) == (int)gridDim.x - 1;
     }
     __syncthreads();
     if (warp == 0 && reinterpret_cast<volatile int *>(red)[0]) {
         // the last CTA: the partials summed in CTA order (lane-strided, then a fixed tree), so the
         // value does not depend on which CTA finished last
-        __threadfence();
         double q = 0.0;
         for (int c = lane; c < (int)gridDim.x; c += 32) q += __ldcg(p.partial + c);
 #pragma unroll
@@ -1377,9 +1400,8 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
                 ok = flag_wait_ge(p.tile_cnt + t, p.slot_ptr[t + 1] - p.slot_ptr[t], p.err, kErrWaitTile);
             sflag[0] = ok ? 1 : 0;
         }
-        __syncthreads();
+        __syncthreads();        // thread 0's acquire loads and this barrier order the reads below
         if (!sflag[0]) return;  // uniform; the error word is set
-        __threadfence();
         // stage: part k covers chunk rows [k ? split : 0, k ? nr : split) of tile t0 + k
         const int ns0 = p.slot_ptr[t0 + 1] - p.slot_ptr[t0];
         const int ns1 = t1 > t0 ? p.slot_ptr[t1 + 1] - p.slot_ptr[t1] : 0;
@@ -1456,7 +1478,6 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
     }
     if (tid < NP) p.sum_part_out[(size_t)c * NP + tid] = colsum;
     if (tid == 0) {
-        __threadfence();
         if (atomicAdd(p.sum_cnt + 1, 1) == G - 1) {  // every CTA is past its waits: reset
             p.sum_cnt[1] = 0;
             atomicExch(p.sum_cnt, 0);
@@ -1803,10 +1824,8 @@ __global__ void __launch_bounds__(kKlThreads)
                 asm volatile("bar.sync 3, 512;" ::: "memory");
             }
         }
-        if (p.X && threadIdx.x == 64) {  // this CTA's denominator entries are out (the fused tails wait)
-            __threadfence();
-            atomicAdd(p.sum_cnt, 1);
-        }
+        if (p.X && threadIdx.x == 64)  // this CTA's denominator entries are out (the fused tails wait)
+            red_release_add(p.sum_cnt, 1);
         const int quarter = warp & 3;     // TMEM lanes this warp may access
         const int part = (warp - 2) >> 2;  // which 32 of the block's 128 columns; also its share of the D2 drain
         const float eps_pos = fmaxf(p.eps, 1e-30f);
@@ -1885,10 +1904,10 @@ __global__ void __launch_bounds__(kKlThreads)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(tempty);
-            if (p.X) {  // this segment's partial product is out: count it on its tile
-                __threadfence();
+            if (p.X) {  // this segment's partial product is out: count it on its tile (the 16 warps'
+                        // stores are ordered before the barrier, one release publishes them)
                 asm volatile("bar.sync 3, 512;" ::: "memory");
-                if (threadIdx.x == 64) atomicAdd(&p.tile_cnt[b / p.kblocks], 1);
+                if (threadIdx.x == 64) red_release_add(&p.tile_cnt[b / p.kblocks], 1);
             }
             seg++;
             b = e;

@@ -126,8 +126,26 @@ __device__ __forceinline__ bool mbar_wait_quiet(uint64_t *bar, uint32_t parity) 
     return true;
 }
 
+// Add to a grid-wide counter with release semantics at GPU scope.  After a barrier of the threads
+// whose global writes it publishes, one thread's release covers all of them (release is
+// cumulative); the reader pairs it with the acquire load of flag_wait_ge and a barrier of its own.
+__device__ __forceinline__ void red_release_add(int *addr, int v) {
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(addr), "r"(v) : "memory");
+}
+
+// Add to a grid-wide counter and return its old value, acquire and release at GPU scope: the
+// caller's earlier writes are published with it, and the writes other threads published with their
+// adds are visible to the caller (and, after a barrier, to its CTA).
+__device__ __forceinline__ int atom_acq_rel_add(int *addr, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(addr), "r"(v) : "memory");
+    return old;
+}
+
 // Bounded wait until the global word at addr (raised by other CTAs of the same grid) is >= target.
 // Returns false (and sets err_bit in *err) on timeout or if another thread already failed.
+// The load is an acquire at GPU scope: after it and a barrier, the CTA's threads see what the
+// releases it observed published.
 __device__ __forceinline__ bool flag_wait_ge(const int *addr, int target, int *err, int err_bit) {
     const long long t0 = clock64();
     for (;;) {
