@@ -375,10 +375,18 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             chunk_denominators<NP, NT>(sX, sG, tid, bar);
         }
         const int t0 = (int)(xb / kTileM), t1 = (int)((xb + nr - 1) / kTileM);  // t1 <= t0 + 1
+        // once past the waits, count this CTA as a reader of the chunk's tiles; the answers are used
+        // at the end of the chunk, where the last reader of a tile resets its counters (every
+        // reader is past its wait by then; the slots themselves stay until the next launch)
+        int rd0 = 0, rd1 = 0;
         if (tid == 0) {
             bool ok = true;
             for (int t = t0; t <= t1 && ok; t++)
                 ok = flag_wait_ge(pr.tile_cnt + t, pr.slot_ptr[t + 1] - pr.slot_ptr[t], err, kErrWaitTile);
+            if (ok) {
+                rd0 = atomicAdd(pr.tile_rd + t0, 1);
+                if (t1 > t0) rd1 = atomicAdd(pr.tile_rd + t1, 1);
+            }
             *sflag = ok ? 1 : 0;
         }
         // the chunk's slot lists (at most kFusedSlots per tile, checked on the host)
@@ -449,13 +457,6 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
                 num[k][q] = v;
             }
         __syncthreads();  // old rows and partial slots read by every thread
-        // count this CTA as a reader of the chunk's tiles; the answers are used at the end of the
-        // chunk (the round trip overlaps the writes): the last reader of a tile resets its counters
-        int rd0 = 0, rd1 = 0;
-        if (tid == 0) {
-            rd0 = atomicAdd(pr.tile_rd + t0, 1);
-            if (t1 > t0) rd1 = atomicAdd(pr.tile_rd + t1, 1);
-        }
 #pragma unroll
         for (int k = 0; k < L::RPT; k++)
 #pragma unroll
@@ -1396,10 +1397,17 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
         const int nr = (int)min(128LL, x1 - xb);
         const int t0 = (int)(xb / kTileM), t1 = (int)((xb + nr - 1) / kTileM);  // t1 <= t0 + 1
         const int split = (int)min((long long)nr, (long long)(t0 + 1) * kTileM - xb);  // rows in t0
+        // once past the waits, count this CTA as a reader of the chunk's tiles; the answers are used
+        // at the end of the chunk, where the last reader of a tile resets its counters
+        int rd0 = 0, rd1 = 0;
         if (tid == 0) {
             bool ok = !first || flag_wait_ge(p.sum_cnt, G, p.err, kErrWaitTile);
             for (int t = t0; t <= t1 && ok; t++)
                 ok = flag_wait_ge(p.tile_cnt + t, p.slot_ptr[t + 1] - p.slot_ptr[t], p.err, kErrWaitTile);
+            if (ok) {
+                rd0 = atomicAdd(p.tile_rd + t0, 1);
+                if (t1 > t0) rd1 = atomicAdd(p.tile_rd + t1, 1);
+            }
             sflag[0] = ok ? 1 : 0;
         }
         __syncthreads();        // thread 0's acquire loads and this barrier order the reads below
@@ -1459,12 +1467,6 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
             sX[rho * LD + a] = xn;
         }
         __syncthreads();
-        if (tid == 0)
-            for (int t = t0; t <= t1; t++)
-                if (atomicAdd(p.tile_rd + t, 1) == p.tile_readers[t] - 1) {  // the last reader resets
-                    p.tile_cnt[t] = 0;
-                    p.tile_rd[t] = 0;
-                }
         // the BF16 copies: Xb (a, row) rows fastest; Xr (row, a) a fastest, zero beyond r
         for (int e = tid; e < r * nr; e += kKlThreads) {
             const int a = e / nr, rho = e - a * nr;
@@ -1476,6 +1478,16 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
         }
         if (tid < NP)
             for (int rho = 0; rho < nr; rho++) colsum += sX[rho * LD + tid];
+        if (tid == 0) {
+            if (rd0 == p.tile_readers[t0] - 1) {
+                p.tile_cnt[t0] = 0;
+                p.tile_rd[t0] = 0;
+            }
+            if (t1 > t0 && rd1 == p.tile_readers[t1] - 1) {
+                p.tile_cnt[t1] = 0;
+                p.tile_rd[t1] = 0;
+            }
+        }
         __syncthreads();
     }
     if (tid < NP) p.sum_part_out[(size_t)c * NP + tid] = colsum;
