@@ -378,8 +378,10 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
         // once past the waits, count this CTA as a reader of the chunk's tiles; the answers are used
         // at the end of the chunk, where the last reader of a tile resets its counters (every
         // reader is past its wait by then; the slots themselves stay until the next launch)
-        int rd0 = 0, rd1 = 0;
+        int rd0 = 0, rd1 = 0, last0 = -1, last1 = -1;
         if (tid == 0) {
+            last0 = pr.tile_readers[t0] - 1;
+            if (t1 > t0) last1 = pr.tile_readers[t1] - 1;
             bool ok = true;
             for (int t = t0; t <= t1 && ok; t++)
                 ok = flag_wait_ge(pr.tile_cnt + t, pr.slot_ptr[t + 1] - pr.slot_ptr[t], err, kErrWaitTile);
@@ -389,11 +391,12 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             }
             *sflag = ok ? 1 : 0;
         }
-        // the chunk's slot lists (at most kFusedSlots per tile, checked on the host)
-        if (tid < 2 && t0 + tid <= t1) {
-            const int t = t0 + tid, q0 = pr.slot_ptr[t], ns = pr.slot_ptr[t + 1] - q0;
-            sSl[tid * (kFusedSlots + 1)] = ns;
-            for (int q = 0; q < ns; q++) sSl[tid * (kFusedSlots + 1) + 1 + q] = pr.slot_list[q0 + q];
+        // the chunk's slot lists (at most kFusedSlots per tile, checked on the host), fetched by two
+        // threads of the second warp while thread 0 waits (they are fixed for the launch)
+        if (tid >= 32 && tid < 34 && t0 + tid - 32 <= t1) {
+            const int u = tid - 32, t = t0 + u, q0 = pr.slot_ptr[t], ns = pr.slot_ptr[t + 1] - q0;
+            sSl[u * (kFusedSlots + 1)] = ns;
+            for (int q = 0; q < ns; q++) sSl[u * (kFusedSlots + 1) + 1 + q] = pr.slot_list[q0 + q];
         }
         __syncthreads();      // thread 0's acquire loads and this barrier order the slot reads below
         if (!*sflag) return;  // uniform
@@ -493,11 +496,11 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
                 for (int k = 0; k < GB; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
         }
         if (tid == 0) {
-            if (rd0 == pr.tile_readers[t0] - 1) {
+            if (rd0 == last0) {
                 pr.tile_cnt[t0] = 0;
                 pr.tile_rd[t0] = 0;
             }
-            if (t1 > t0 && rd1 == pr.tile_readers[t1] - 1) {
+            if (t1 > t0 && rd1 == last1) {
                 pr.tile_cnt[t1] = 0;
                 pr.tile_rd[t1] = 0;
             }
@@ -1399,8 +1402,10 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
         const int split = (int)min((long long)nr, (long long)(t0 + 1) * kTileM - xb);  // rows in t0
         // once past the waits, count this CTA as a reader of the chunk's tiles; the answers are used
         // at the end of the chunk, where the last reader of a tile resets its counters
-        int rd0 = 0, rd1 = 0;
+        int rd0 = 0, rd1 = 0, last0 = -1, last1 = -1;
         if (tid == 0) {
+            last0 = p.tile_readers[t0] - 1;
+            if (t1 > t0) last1 = p.tile_readers[t1] - 1;
             bool ok = !first || flag_wait_ge(p.sum_cnt, G, p.err, kErrWaitTile);
             for (int t = t0; t <= t1 && ok; t++)
                 ok = flag_wait_ge(p.tile_cnt + t, p.slot_ptr[t + 1] - p.slot_ptr[t], p.err, kErrWaitTile);
@@ -1479,11 +1484,11 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
         if (tid < NP)
             for (int rho = 0; rho < nr; rho++) colsum += sX[rho * LD + tid];
         if (tid == 0) {
-            if (rd0 == p.tile_readers[t0] - 1) {
+            if (rd0 == last0) {
                 p.tile_cnt[t0] = 0;
                 p.tile_rd[t0] = 0;
             }
-            if (t1 > t0 && rd1 == p.tile_readers[t1] - 1) {
+            if (t1 > t0 && rd1 == last1) {
                 p.tile_cnt[t1] = 0;
                 p.tile_rd[t1] = 0;
             }
