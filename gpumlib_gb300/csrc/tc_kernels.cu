@@ -506,10 +506,22 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             }
         }
     }
+    // the next launch reads entry (i, k), i <= k, at k * NP + i: only blocks that reach that triangle
+    // are written, GB values at a time
+    if (ga0 + GB - 1 >= gb0) {
 #pragma unroll
-    for (int i = 0; i < GB; i++)
+        for (int i = 0; i < GB; i++) {
+            float *dst = gpc + (ga0 + i) * NP + gb0;
+            if constexpr (GB == 4) {
+                *reinterpret_cast<float4 *>(dst) = make_float4(gacc[i][0], gacc[i][1], gacc[i][2], gacc[i][3]);
+            } else if constexpr (GB == 2) {
+                *reinterpret_cast<float2 *>(dst) = make_float2(gacc[i][0], gacc[i][1]);
+            } else {
 #pragma unroll
-        for (int k = 0; k < GB; k++) gpc[(ga0 + i) * NP + gb0 + k] = gacc[i][k];
+                for (int k = 0; k < GB; k++) dst[k] = gacc[i][k];
+            }
+        }
+    }
 }
 
 // Gram partials of a factor for the first fused kernel: CTA c over rows [c*rows/G, (c+1)*rows/G),
