@@ -485,7 +485,7 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             }
         }
         // this chunk's new rows into this CTA's Gram partial, rows in order
-#pragma unroll 2
+#pragma unroll 4
         for (int rr = 0; rr < nr; rr++) {
             float xa[GB], xb2[GB];
             lds_vec<GB>(sX + rr * L::LDX + ga0, xa);
