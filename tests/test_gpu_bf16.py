@@ -34,8 +34,11 @@ def emulate_one(V, W, H, eps, H1_gpu):
     return W1, H1
 
 
+# The last two run the fused half-step kernel with more than 64 factor rows per CTA in one half-step
+# (20000 rows over 152 CTAs: three chunks in the update tail); the first one is not fused (19 stream-K
+# segments per tile in its H-step, above the fused tail's 15).
 SHAPES = [(8192, 1024, 64), (1000, 777, 20), (300, 1300, 7), (129, 65, 16), (64, 64, 1), (2048, 4096, 128),
-          (513, 2047, 176), (37, 11, 3)]
+          (513, 2047, 176), (37, 11, 3), (20000, 2048, 32), (2048, 20000, 64)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=["%dx%dr%d" % s for s in SHAPES])
