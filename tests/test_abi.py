@@ -161,3 +161,62 @@ int main() {
     return 0;
 }
 """
+
+
+def header_prototypes():
+    """{name: (return type, [parameter types])} of every function include/gpunmf.h declares."""
+    text = open(os.path.join(ROOT, "include", "gpunmf.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for ret, name, params in re.findall(r"\b([A-Za-z_][\w ]*?\**)\s*\b((?:gpunmf|gpumlib)_\w+)\s*\(([^;{]*?)\)\s*;",
+                                        text, flags=re.S):
+        ps = [] if params.strip() in ("", "void") else [re.sub(r"\s+", " ", p.strip()) for p in params.split(",")]
+        # drop the parameter name, keep the type
+        types = [re.sub(r"\s*\b\w+$", "", p) if not p.endswith("*") else p for p in ps]
+        ret = re.sub(r"^(?:extern\s+\"C\"\s+|GPUNMF_API\s+)", "", ret.strip())
+        out[name] = (ret.strip(), types)
+    return out
+
+
+def _kind_of_c(t):
+    """Canonical kind of a C type: 'ptr', 'dim3', 'void', or (class, bytes, signed)."""
+    t = t.replace("const ", "").strip()
+    if "*" in t or t in ("gpunmf_handle",):
+        return "ptr"
+    size_t = ctypes.sizeof(ctypes.c_size_t)
+    return {"int": ("int", 4, True), "unsigned int": ("int", 4, False), "unsigned": ("int", 4, False),
+            "long long": ("int", 8, True), "unsigned long long": ("int", 8, False), "size_t": ("int", size_t, False),
+            "float": ("float", 4, True), "double": ("float", 8, True), "gpunmf_dim3": "dim3", "void": "void",
+            # the header's enums are passed and returned as int
+            "gpunmf_status": ("int", 4, True), "gpunmf_rule": ("int", 4, True),
+            "gpunmf_precision": ("int", 4, True)}[t]
+
+
+def _kind_of_ctypes(c):
+    from gpumlib_gb300 import _native
+    if c is None:
+        return "void"
+    if c in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(c, ctypes._Pointer):
+        return "ptr"
+    if c is _native.Dim3:
+        return "dim3"
+    code = c._type_
+    if code in "fd":
+        return ("float", ctypes.sizeof(c), True)
+    return ("int", ctypes.sizeof(c), code.islower())
+
+
+def test_ctypes_signatures_match_header():
+    """Every header function has a ctypes signature with the same arity, argument kinds and return kind."""
+    from gpumlib_gb300 import _native
+    protos = header_prototypes()
+    assert len(protos) >= 50
+    sigs = {name: (res, args) for name, res, args in _native.SIGNATURES}
+    assert sorted(protos) == sorted(sigs), set(protos) ^ set(sigs)
+    for name, (ret, params) in protos.items():
+        res, args = sigs[name]
+        assert len(args) == len(params), (name, params, args)
+        for k, (p, a) in enumerate(zip(params, args)):
+            assert _kind_of_c(p) == _kind_of_ctypes(a), (name, k, p, a)
+        assert _kind_of_c(ret) == _kind_of_ctypes(res), (name, ret, res)
