@@ -18,7 +18,7 @@
  * them, nmf_multiplicative_euclidian.cpp:45,66); the random constructor
  * draws W and H from a seeded counter-based generator (the reference uses
  * an unseeded rand(), nmf_base.h:56-61).
- * Additions: Residual() (FP64 relative Frobenius residual on the GPU),
+ * Additions: Residual() (FP64 relative Frobenius residual on the GPU), ObjectiveKL(),
  * Iterate(k), SetQualityInterval(k), and optional eps / precision
  * arguments on every constructor.
  */
@@ -142,6 +142,12 @@ class NMF {
         double r = 0.0;
         nmf_check(gpunmf_residual_fp64(h_, &r));
         return r;
+    }
+    //! Generalised KL objective sum V log(V / WH) - V + WH, FP64 on the GPU (any rule).
+    double ObjectiveKL() {
+        double o = 0.0;
+        nmf_check(gpunmf_objective_kl_fp64(h_, &o));
+        return o;
     }
     gpunmf_handle Handle() const { return h_; }
 

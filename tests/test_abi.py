@@ -148,7 +148,7 @@ int main() {
         NMF_MultiplicativeDivergence kl(V, W, H);
         kl.DoIteration(true); kl.DoIteration(false);
         HostMatrix<cudafloat> kw = kl.GetW();
-        std::printf("%.9g\n", kw(1, 1));
+        std::printf("%.9g %.12g\n", kw(1, 1), kl.ObjectiveKL());
         NMF_AdditiveEuclidian ae(V, W, H);          // the reference GPU class: H stays as given
         NMF_AdditiveEuclidian ae2(V, W, H, true);   // H updated as well
         NMF_AdditiveDivergence ad(V, W, H);
