@@ -15,11 +15,12 @@ Arms:
                      DoIteration, then GetW/GetH (D2H), all inside the timed
                      region.
   --impl reference   the reference's CPU NMF (HostNMF.h:64-114) on the host
-                     cores: the oracle's transcription (or the reference's
-                     own build where present), all host threads.  Each step
-                     is one iteration of the same rule on a 128-column slice
-                     of the same V (W full, H sliced), scaled to full-size
-                     iterations by the ratio of their multiply-add counts.
+                     cores: the oracle's float transcription, which gives the
+                     reference HostNMF's bits (pinned by golden vectors made
+                     with the reference's own build), split over all host
+                     threads by output element.  Each step is one full-size
+                     iteration of the same workload (no slicing, nothing
+                     extrapolated).
 
 Multi-GPU: the path does not shard (one factorisation per GPU), so --gpus N
 runs N independent replicas (one per rank, launched by torchrun) and reports
@@ -68,9 +69,13 @@ def parse():
     p.add_argument("--r", type=int, default=64)
     p.add_argument("--full-job-iters", type=int, default=500,
                    help="iterations of the residual comparison job (0 = skip)")
+    p.add_argument("--err-iters", type=int, default=3,
+                   help="iterations after which W, H, W H are compared with the FP64 oracle (0 = skip)")
+    p.add_argument("--kl-lam-scale", type=float, default=1.0,
+                   help="KL workload: Poisson means scaled by this (0.01 gives ~89%% zeros)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", choices=["large_euclidean", "batched", "serving", "kl_counts"],
+    p.add_argument("--workload", choices=["large_euclidean", "batched", "serving", "kl_counts", "plain_small"],
                    default="large_euclidean")
     p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--serve-duration", type=float, default=5.0,
@@ -118,6 +123,18 @@ class Dist:
     def close(self):
         if self.world > 1:
             self.td.destroy_process_group()
+
+
+FP32_SMS = 152
+
+
+def peak_sm_mhz():
+    """The GPU's maximum SM clock (MEASURED_PEAKS.json), else GB300's 2070 MHz."""
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        return 2070.0
 
 
 def peaks():
@@ -212,31 +229,32 @@ def timed_repeats(measure, dist, clk, min_seconds=1.0, max_reps=500):
                                       "ms_min": round(min(times), 4), "ms_max": round(max(times), 4)}
 
 
-def euclid_madds(n, m, r):
-    # W'V, W'W, W'W H, V H', H H', W H H'  (multiply-adds)
-    return 2 * n * m * r + r * r * n + r * r * m + r * r * m + n * r * r + n * r * r
+def workload_config(n, m, r, eps, world, rule="euclidean", **extra):
+    """The `config` object of a workload, the same dict on both arms (the engine's arithmetic is
+    reported in `dtype` / `precision`, outside it)."""
+    cfg = {"workload": "large_euclidean_%dx%d_r%d" % (n, m, r) if rule == "euclidean" else
+           "kl_counts_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r, "rule": rule, "eps": eps,
+           "parallelism": "replicas" if world > 1 else "single",
+           "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16 > 129 MB); no flush" %
+                 (n * m * 4 >> 20, n * m * 2 >> 20)}
+    cfg.update(extra)
+    return cfg
 
 
-def cpu_reference_steps(V, W, H, r, steps, warmup, slice_cols=128, min_seconds=0.0):
-    """Time the reference CPU iteration on a column slice (at least `steps` iterations and, if given,
-    at least min_seconds of CPU work); returns (iters/s full-size, info)."""
+def cpu_reference_steps(V, W, H, eps, steps, warmup, min_seconds=0.0, rule=0):
+    """Time full-size iterations of the reference's CPU NMF (HostNMF.h:64-150) on all host threads:
+    at least `steps` iterations and, if given, at least min_seconds of CPU work.  The oracle's float
+    transcription is used: it gives the reference build's bits (golden vectors) and splits each
+    product over threads by output element (the reference's HostNMF is single-threaded).
+    Returns (iters/s, seconds per iteration, info)."""
     import oracle
-    n, m = V.shape
-    mc = min(slice_cols, m)
-    Vs = np.asfortranarray(V[:, :mc])
-    Hs = np.asfortranarray(H[:, :mc])
     threads = os.cpu_count() or 1
-    use_ref = oracle.ref() is not None
-    kind = "reference" if use_ref else "port"
-    Wc, Hc = W.copy(order="F"), Hs.copy(order="F")
+    Wc, Hc = W.copy(order="F"), H.copy(order="F")
 
     def one():
         nonlocal Wc, Hc
-        if use_ref:
-            # the reference build is single-threaded (HostNMF has no threading)
-            Wc, Hc = oracle.reference_run(0, Vs, Wc, Hc, 1)
-        else:
-            Wc, Hc = oracle.hostnmf_run(0, Vs, Wc, Hc, 1, eps=np.float32(1e-9), nthreads=threads)
+        Wc, Hc = oracle.hostnmf_run(rule, V, Wc, Hc, 1, eps=np.float32(eps), nthreads=threads,
+                                    clamp_sums=(rule == 1))
 
     for _ in range(warmup):
         one()
@@ -246,14 +264,26 @@ def cpu_reference_steps(V, W, H, r, steps, warmup, slice_cols=128, min_seconds=0
         one()
         done += 1
     dt = time.perf_counter() - t0
-    steps = done
-    scale = euclid_madds(n, mc, r) / euclid_madds(n, m, r)
-    ips = steps * scale / dt
-    info = {"kind": kind, "cores": 1 if use_ref else threads,
-            "sample": "%d iterations of the %dx%d slice (r=%d) of V; scaled by multiply-adds %.5f of a full "
-                      "%dx%d iteration" % (steps, n, mc, r, scale, n, m),
-            "seconds": dt}
-    return ips, info
+    n, m = V.shape
+    info = {"kind": "port", "cores": threads,
+            "sample": "%d full %dx%d iterations (r=%d) of the same workload, after %d warm-up; the "
+                      "reference HostNMF's arithmetic (bit-identical transcription) split over %d host threads"
+                      % (done, n, m, W.shape[1], warmup, threads),
+            "seconds": round(dt, 3), "iterations": done}
+    return done / dt, dt / done, info
+
+
+def error_vs_f64(rule, V, W, H, eps, iters, gpu_factors):
+    """W, H and W H of each precision after `iters` iterations from the workload's W/H, against the
+    FP64 oracle's (the GPU classes' rules in double precision) after the same iterations."""
+    import oracle
+    t0 = time.perf_counter()
+    Wd, Hd = oracle.f64_run_blas(rule, V, W, H, iters, eps=eps)
+    out = {"iters": iters}
+    for prec, (Wg, Hg) in gpu_factors.items():
+        out[prec] = {k: float("%.4g" % v) for k, v in oracle.factor_errors(Wg, Hg, Wd, Hd).items()}
+    out["oracle"] = "FP64 CPU restatement of the GPU rules (BLAS products), %.1f s" % (time.perf_counter() - t0)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -337,38 +367,46 @@ def run_ours(args, rank, world, local, dist):
     out = {"metric": METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if precision == "bf16" else "f32",
+           "precision": precision,
            "data": "synthetic: V = A B + |N(0,0.01)|, A,B ~ Gamma(2,0.5) (seed 2); W,H U[0,1)+1e-4 (seed 3)",
-           "config": {"workload": "large_euclidean_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r,
-                      "rule": "euclidean", "precision": precision, "eps": eps,
-                      "parallelism": "replicas" if world > 1 else "single",
-                      "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16 > 129 MB); no flush" %
-                            (n * m * 4 >> 20, n * m * 2 >> 20)},
+           "config": workload_config(n, m, r, eps, world),
            "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roofline}
 
     # end to end through the public API from pinned host buffers
     if not args.no_e2e:
         out["e2e"] = run_e2e(lib, g, V, W, H, eps, precision, args, dist, world)
 
-    # equal-residual check: a full job in each precision
-    if args.full_job_iters and rank == 0:
-        res = {}
-        for prec in (["bf16", "fp32"] if precision == "bf16" else ["fp32"]):
-            with g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=prec, quality_interval=0) as j:
-                tt = j.TimeIterations(args.full_job_iters)
-                res[prec] = {"residual": j.Residual(), "iters_per_s": round(args.full_job_iters / (tt["total_ms"] / 1e3), 2)}
-        out["full_job"] = {"iters": args.full_job_iters, **res}
-        if "bf16" in res:
-            out["full_job"]["residual_gap"] = abs(res["bf16"]["residual"] - res["fp32"]["residual"])
-            out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 3)
+    # equal-residual check: a full job in each precision, and the error of W, H and W H against the
+    # FP64 oracle after a few iterations from the same start
+    if rank == 0:
+        precs = ["bf16", "fp32"] if precision == "bf16" else ["fp32"]
+        if args.full_job_iters:
+            res = {}
+            for prec in precs:
+                with g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=prec, quality_interval=0) as j:
+                    tt = j.TimeIterations(args.full_job_iters)
+                    res[prec] = {"residual": j.Residual(),
+                                 "iters_per_s": round(args.full_job_iters / (tt["total_ms"] / 1e3), 2)}
+            out["full_job"] = {"iters": args.full_job_iters, **res}
+            if "bf16" in res:
+                out["full_job"]["residual_gap"] = abs(res["bf16"]["residual"] - res["fp32"]["residual"])
+                out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 3)
+        if args.err_iters:
+            facs = {}
+            for prec in precs:
+                with g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=prec, quality_interval=0) as j:
+                    j.Iterate(args.err_iters)
+                    facs[prec] = (j.GetW(), j.GetH())
+            out["err_vs_f64"] = error_vs_f64(0, V, W, H, eps, args.err_iters, facs)
 
     if rank == 0 and not args.no_cpu_baseline:
-        # a bounded sample of about 10 s of host-core work: iterations of a 1024-column slice
-        ips, info = cpu_reference_steps(V, W, H, r, steps=3, warmup=1, slice_cols=1024, min_seconds=10.0)
+        # a bounded sample of about 10 s of host-core work: full-size iterations
+        ips, _, info = cpu_reference_steps(V, W, H, eps, steps=1, warmup=1, min_seconds=10.0)
         out["cpu_baseline"] = {"value": ips, "unit": "iters/s", **info}
     return out
 
 
-def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world):
+def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world, iters=None, make=None):
     import ctypes
     n, m = V.shape
     r = W.shape[1]
@@ -387,8 +425,11 @@ def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world):
         oH = pinned(np.zeros_like(H))
         from gpumlib_gb300 import _native
 
+        steps = iters or args.steps
+        ctor = make or g.NMF_MultiplicativeEuclidianDistance
+
         def job(iters):
-            nmf = g.NMF_MultiplicativeEuclidianDistance(hV, hW, hH, eps=eps, precision=precision)
+            nmf = ctor(hV, hW, hH, eps=eps, precision=precision)
             for _ in range(iters):
                 nmf.DoIteration()            # per-iteration quality read-back (4 bytes D2H)
                 nmf.QualityImprovement()
@@ -401,20 +442,99 @@ def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world):
         job(max(1, args.warmup)).close()
         dist.barrier()
         t0 = time.perf_counter()
-        nmf = job(args.steps)
+        nmf = job(steps)
         dt = time.perf_counter() - t0
         nmf.close()
         dt = dist.max(dt)
         h2d = V.nbytes + W.nbytes + H.nbytes
-        d2h = W.nbytes + H.nbytes + 4 * args.steps
-        return {"value": round(world * args.steps / dt, 2), "unit": "iters/s",
-                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+        d2h = W.nbytes + H.nbytes + 4 * steps
+        return {"value": round(world * steps / dt, 2), "unit": "iters/s",
+                "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps,
                 "note": "one job of %d iterations from pinned host buffers, after one untimed warm-up job: create "
                         "(H2D V,W,H), iterations with quality read-back, GetW/GetH (D2H); bytes amortised per step"
-                        % args.steps}
+                        % steps}
     finally:
         for p in bufs:
             lib.gpunmf_host_free(p)
+
+
+# ---------------------------------------------------------------------------
+# plain FP32 workload: V 1024 x 512, r = 16, 200 iterations, residual every iteration
+# ---------------------------------------------------------------------------
+PLAIN_METRIC = "NMF iters/s, plain FP32 Euclidean multiplicative update, V 1024x512, r=16, 200 iterations"
+
+
+def run_plain(args, rank, world, local, dist):
+    import gpumlib_gb300 as g
+    from gpumlib_gb300 import _native, inputs
+    import oracle
+
+    lib = _native.load()
+    cfg = inputs.plain_euclidean_1024x512()
+    V, W, H, eps, iters = cfg["V"], cfg["W"], cfg["H"], cfg["eps"], cfg["iters"]
+    n, m = V.shape
+    r = cfg["r"]
+    prec = args.precision or "fp32"
+    # device-timed: a step is one iteration (inputs resident), the timed loop repeated as for the
+    # large workload
+    nmf = g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=prec, quality_interval=0)
+    nmf.Iterate(args.warmup)
+    nmf.Synchronize()
+    dist.barrier()
+    with ClockSampler(local) as clk:
+        t = {}
+
+        def measure():
+            t.update(nmf.TimeIterations(args.steps))
+            return t["total_ms"]
+
+        ms, rep_info = timed_repeats(measure, dist, clk)
+    nmf.close()
+    value = world * args.steps / (ms / 1e3)
+    out = {"metric": PLAIN_METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16" if prec == "bf16" else "f32", "precision": prec,
+           "data": "synthetic: V U[0,1) (seed 0); W,H U[0,1)+1e-4 (seed 1)",
+           "config": {"workload": "plain_euclidean_1024x512_r16", "n": n, "m": m, "r": r, "rule": "euclidean",
+                      "eps": eps, "iters": iters, "parallelism": "replicas" if world > 1 else "single",
+                      "l2": "V 2 MB fits L2: a launch-bound workload; no flush"},
+           "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"]}
+    if rank == 0:
+        # the whole 200-iteration job with the residual read after every iteration, against the
+        # reference HostNMF's trajectory (its own build where present, else the bit-identical port)
+        traj = []
+        with g.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision=prec, quality_interval=0) as j:
+            for _ in range(iters):
+                j.DoIteration()
+                traj.append(j.Residual())
+            Wg, Hg = j.GetW(), j.GetH()
+        threads = os.cpu_count() or 1
+        Wo, Ho, otraj = oracle.hostnmf_run(0, V, W, H, iters, eps=np.float32(eps), nthreads=threads, residuals=True)
+        traj = np.array(traj)
+        out["residual_per_iteration"] = [float("%.7g" % x) for x in traj]
+        out["vs_reference_cpu"] = {
+            "max_rel_residual_diff": float(np.max(np.abs(traj - otraj) / otraj)),
+            "WH": oracle.factor_errors(Wg, Hg, Wo.astype(np.float64), Ho.astype(np.float64))["WH"],
+            "against": "reference HostNMF arithmetic (float transcription, golden-pinned), same eps"}
+        if not args.no_cpu_baseline:
+            # the reference's CPU NMF timed over the full 200-iteration job (its own build, which has
+            # its eps built in at 1e-8 -- the cost does not depend on it -- where present)
+            if oracle.ref() is not None:
+                t0 = time.perf_counter()
+                oracle.reference_run(0, V, W, H, iters)
+                dt = time.perf_counter() - t0
+                kind, cores = "reference", 1
+            else:
+                t0 = time.perf_counter()
+                oracle.hostnmf_run(0, V, W, H, iters, eps=np.float32(eps), nthreads=threads)
+                dt = time.perf_counter() - t0
+                kind, cores = "port", threads
+            out["cpu_baseline"] = {"value": iters / dt, "unit": "iters/s", "kind": kind, "cores": cores,
+                                   "sample": "the full %d-iteration job" % iters, "seconds": round(dt, 3)}
+        if not args.no_e2e:
+            out["e2e"] = run_e2e(lib, g, V, W, H, eps, prec, args, dist, world, iters=iters)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -469,6 +589,8 @@ def run_batched(args, rank, world, local, dist):
     sample = [insts[k] for k in range(0, count, max(1, count // args.baseline_sample))][:args.baseline_sample]
     _, base_s = gb.run_one_per_instance(sample, iters)
     base_jobs_s = len(sample) / base_s
+    fp32_mhz = peak_sm_mhz()
+    fp32_peak = FP32_SMS * 128 * 2 * fp32_mhz * 1e6 / 1e12
     total_madds = sum(2 * n * m * r + 2 * r * r * (n + m) for (n, m, r) in (d["V"].shape + (d["W"].shape[1],)
                                                                           for d in insts)) * iters
     out = {"metric": BATCH_METRIC, "value": round(value, 1), "unit": "jobs/s", "n_gpus": world,
@@ -480,7 +602,11 @@ def run_batched(args, rank, world, local, dist):
                       "l2": "each step re-reads every instance's V 2x per iteration; working set %.2f GB > L2" %
                             (sum(d["V"].nbytes for d in insts) / 1e9)},
            "clocks": clk.summary(), "gpu_launches": args.steps,
-           "roofline": {"bound": "fp32-simt", "achieved_tflops": round(2 * total_madds / (ms / 1e3) / 1e12, 2),
+           "roofline": {"bound": "fp32-simt", "achieved": round(2 * total_madds / (ms / 1e3) / 1e12, 2),
+                        "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
+                        "frac": round(2 * total_madds / (ms / 1e3) / 1e12 / fp32_peak, 4),
+                        "peak_source": "computed: %d SMs x 128 FP32 lanes x 2 flop x %.0f MHz (no measured FP32 "
+                                       "figure exists for this GPU)" % (FP32_SMS, fp32_mhz),
                         "note": "FP32 CUDA-core arithmetic; V served mostly from L2 (instances in flight)"},
            "autotune": {"%d/%d" % k: v[0] for k, v in table.items()}, "autotune_s": round(tune_s, 2),
            "create_s": round(create_s, 2),
@@ -502,7 +628,7 @@ def run_kl(args, rank, world, local, dist):
     import gpumlib_gb300 as g
     from gpumlib_gb300 import inputs
 
-    cfg = inputs.kl_counts()
+    cfg = inputs.kl_counts(lam_scale=args.kl_lam_scale)
     V, W, H, eps = cfg["V"], cfg["W"], cfg["H"], cfg["eps"]
     n, m = V.shape
     r = cfg["r"]
@@ -541,23 +667,35 @@ def run_kl(args, rank, world, local, dist):
     out = {"metric": KL_METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if prec == "bf16" else "f32",
-           "data": "synthetic: V ~ Poisson(P Q), P 16384x128, Q 128x4096 ~ Gamma(0.3,1) (seed 4); W,H U[0,1)+1e-4 (seed 5)",
-           "config": {"workload": "kl_counts_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r, "rule": "kl",
-                      "precision": prec, "eps": eps, "zero_fraction": float(np.mean(V == 0)),
-                      "l2": "inputs larger than L2 (V %d MB fp32 / %d MB bf16)" % (n * m * 4 >> 20, n * m * 2 >> 20)},
+           "precision": prec,
+           "data": "synthetic: V ~ Poisson(%sP Q), P 16384x128, Q 128x4096 ~ Gamma(0.3,1) (seed 4); W,H U[0,1)+1e-4 "
+                   "(seed 5)" % ("" if args.kl_lam_scale == 1.0 else "%g " % args.kl_lam_scale),
+           "config": workload_config(n, m, r, eps, world, rule="kl", lam_scale=args.kl_lam_scale,
+                                     zero_fraction=round(float(np.mean(V == 0)), 5)),
            "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roof}
-    if args.full_job_iters and rank == 0:
-        iters = min(args.full_job_iters, cfg["iters"])
-        res = {}
-        for pr in (["bf16", "fp32"] if prec == "bf16" else ["fp32"]):
-            with g.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision=pr, quality_interval=0) as j:
-                tt = j.TimeIterations(iters)
-                res[pr] = {"residual": j.Residual(), "kl_objective": j.ObjectiveKL(),
-                           "iters_per_s": round(iters / (tt["total_ms"] / 1e3), 2)}
-        out["full_job"] = {"iters": iters, **res}
-        if "bf16" in res:
-            out["full_job"]["residual_gap"] = abs(res["bf16"]["residual"] - res["fp32"]["residual"])
-            out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 2)
+    if args.kl_lam_scale != 1.0:
+        out["config"]["workload"] += "_lam%g" % args.kl_lam_scale
+    if rank == 0:
+        precs = ["bf16", "fp32"] if prec == "bf16" else ["fp32"]
+        if args.full_job_iters:
+            iters = min(args.full_job_iters, cfg["iters"])
+            res = {}
+            for pr in precs:
+                with g.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision=pr, quality_interval=0) as j:
+                    tt = j.TimeIterations(iters)
+                    res[pr] = {"residual": j.Residual(), "kl_objective": j.ObjectiveKL(),
+                               "iters_per_s": round(iters / (tt["total_ms"] / 1e3), 2)}
+            out["full_job"] = {"iters": iters, **res}
+            if "bf16" in res:
+                out["full_job"]["residual_gap"] = abs(res["bf16"]["residual"] - res["fp32"]["residual"])
+                out["full_job"]["speedup_vs_fp32"] = round(res["bf16"]["iters_per_s"] / res["fp32"]["iters_per_s"], 2)
+        if args.err_iters:
+            facs = {}
+            for pr in precs:
+                with g.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision=pr, quality_interval=0) as j:
+                    j.Iterate(args.err_iters)
+                    facs[pr] = (j.GetW(), j.GetH())
+            out["err_vs_f64"] = error_vs_f64(1, V, W, H, eps, args.err_iters, facs)
     return out
 
 
@@ -607,13 +745,13 @@ def run_reference(args, rank, world):
         return None
     n, m, r = args.n, args.m, args.r
     V, W, H, eps = make_workload(n, m, r)
-    ips, info = cpu_reference_steps(V, W, H, r, steps=max(1, args.steps), warmup=max(0, min(args.warmup, 2)))
+    # every step (and every warm-up step) is one full-size iteration
+    ips, sec, info = cpu_reference_steps(V, W, H, eps, steps=max(1, args.steps), warmup=max(0, args.warmup))
     return {"impl": "reference", "metric": METRIC, "value": ips, "unit": "iters/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / ips if ips else None,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "steps": info["iterations"], "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "precision": "fp32",
             "data": "synthetic (same workload as the engine arm)",
-            "config": {"workload": "large_euclidean_%dx%d_r%d" % (n, m, r), "n": n, "m": m, "r": r,
-                       "rule": "euclidean", "precision": "fp32"},
+            "config": workload_config(n, m, r, eps, world),
             "cpu_baseline": {"value": ips, "unit": "iters/s", **info},
             "e2e": {"value": ips, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -636,6 +774,8 @@ def main():
             out = run_serving(args, rank, world, local, dist)
         elif args.workload == "kl_counts":
             out = run_kl(args, rank, world, local, dist)
+        elif args.workload == "plain_small":
+            out = run_plain(args, rank, world, local, dist)
         else:
             out = run_ours(args, rank, world, local, dist)
     finally:

@@ -31,6 +31,9 @@ SIGNATURES = [
     ("gpunmf_destroy", ctypes.c_int, [ctypes.c_void_p]),
     ("gpunmf_iterate", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     ("gpunmf_set_quality_interval", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("gpunmf_set_wait_limit_cycles", ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
+    ("gpunmf_inject_missing_arrival", ctypes.c_int, [ctypes.c_void_p]),
+    ("gpunmf_set_grid_limit", ctypes.c_int, [ctypes.c_int]),
     ("gpunmf_quality_improvement", ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     ("gpunmf_residual_fp64", ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     ("gpunmf_objective_kl_fp64", ctypes.c_int, [ctypes.c_void_p, c_double_p]),
@@ -77,6 +80,8 @@ SIGNATURES = [
                                            ctypes.POINTER(ctypes.c_size_t)]),
     ("gpunmf_server_clock", ctypes.c_double, [ctypes.c_void_p]),
     ("gpunmf_server_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gpunmf_server_generate", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_ulonglong, ctypes.c_float] +
+     [ctypes.c_void_p] * 4),
     ("gpunmf_grouped_train", ctypes.c_int,
      [ctypes.c_int] * 5 + [ctypes.c_void_p] * 3 + [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int,
                                                     ctypes.c_void_p]),

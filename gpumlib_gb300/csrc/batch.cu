@@ -657,8 +657,12 @@ gpunmf_status gpunmf_batch_run(gpunmf_batch *b, int iters) {
         GPUNMF_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         gpunmf_status st = batch_launch(b, iters);
         cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-        if (st != GPUNMF_OK) return st;
-        GPUNMF_CUDA_TRY(e);
+        if (st != GPUNMF_OK || e != cudaSuccess) {
+            // the capture may have produced a graph even when the launch or the capture failed
+            if (g) cudaGraphDestroy(g);
+            if (st != GPUNMF_OK) return st;
+            GPUNMF_CUDA_TRY(e);
+        }
         e = cudaGraphInstantiate(&b->graph, g, 0);
         cudaGraphDestroy(g);
         GPUNMF_CUDA_TRY(e);

@@ -614,6 +614,34 @@ gpunmf_status gpunmf_set_quality_interval(gpunmf_handle h, int interval) {
     return GPUNMF_OK;
 }
 
+gpunmf_status gpunmf_set_wait_limit_cycles(gpunmf_handle h, long long cycles) {
+    CHECK_HANDLE(h);
+    if (h->precision != GPUNMF_BF16) {
+        set_error("only the BF16 tensor-core kernels wait on one another");
+        return GPUNMF_ERR_UNSUPPORTED;
+    }
+    tc_set_wait_limit(h, cycles);
+    return GPUNMF_OK;
+}
+
+gpunmf_status gpunmf_inject_missing_arrival(gpunmf_handle h) {
+    CHECK_HANDLE(h);
+    if (h->precision != GPUNMF_BF16) {
+        set_error("only the BF16 tensor-core kernels count tile arrivals");
+        return GPUNMF_ERR_UNSUPPORTED;
+    }
+    return tc_inject_missing_arrival(h);
+}
+
+gpunmf_status gpunmf_set_grid_limit(int ctas) {
+    if (ctas < 0) {
+        set_error("grid limit must be >= 0");
+        return GPUNMF_ERR_INVALID;
+    }
+    tc_set_grid_limit(ctas);
+    return GPUNMF_OK;
+}
+
 gpunmf_status gpunmf_quality_improvement(gpunmf_handle h, float *out) {
     CHECK_HANDLE(h);
     if (!out) return GPUNMF_ERR_INVALID;

@@ -93,5 +93,8 @@ bool tc_quality_ready(const gpunmf_job *j);
 bool tc_quality_writes_host(const gpunmf_job *j);
 gpunmf_status tc_quality(gpunmf_job *j);
 gpunmf_status tc_check(gpunmf_job *j);    // reads the kernels' error word (after a sync)
+void tc_set_wait_limit(gpunmf_job *j, long long cycles);  // <= 0: the default (about 2 s)
+gpunmf_status tc_inject_missing_arrival(gpunmf_job *j);
+void tc_set_grid_limit(int ctas);         // CTAs per launch of jobs created later (0: one per SM)
 void tc_destroy(gpunmf_job *j);
 }  // namespace gpunmf

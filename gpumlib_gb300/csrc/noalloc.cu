@@ -14,15 +14,18 @@
 // Limits and sharing:
 //  * the array holds kNoAllocMaxCtas pairs (1 MiB); a shape whose product
 //    needs more CTAs is rejected with GPUNMF_ERR_INVALID;
-//  * the array is a file-scope __device__ variable, so every GPU that loads
-//    the library holds it until the process exits;
+//  * the array is a file-scope static __device__ variable, so every GPU that
+//    loads the library holds it until the process exits;
 //  * every call uses the same array and it keeps the last call's contents;
 //    a call writes every partial it later reads, so nothing needs clearing,
 //    but calls that overlap on the GPU (different streams, or threads) race
 //    on it and must be serialised by the caller;
 //  * the first call on each device looks the array's device address up with
 //    cudaGetSymbolAddress (host code cannot use the array's name as a device
-//    pointer); make that first call before any stream capture begins.
+//    pointer); make that first call before any stream capture begins;
+//  * the looked-up address is kept for the life of the process, so the entry
+//    point must not be used on a device after cudaDeviceReset() on it (the
+//    reset unloads the module and the kept address no longer names the array).
 #include <mutex>
 
 #include "common.cuh"
@@ -33,12 +36,12 @@ namespace {
 constexpr int kNoAllocMaxCtas = 65536;
 constexpr int kMaxDevices = 64;
 
-__device__ __align__(256) double g_residual_scratch[2 * kNoAllocMaxCtas];
-
 std::mutex g_scratch_mu;
 double *g_scratch_addr[kMaxDevices] = {};
 
 }  // namespace
+
+static __device__ __align__(256) double g_residual_scratch[2 * kNoAllocMaxCtas];
 
 using namespace gpunmf;
 

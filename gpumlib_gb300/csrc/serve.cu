@@ -67,19 +67,25 @@ static int gen_blocks(long long count) {
     return (int)std::min<long long>(std::max<long long>(b, 1), 4 * kNumSMsGB300);
 }
 
-// fills j->V, j->W, j->H on the job's stream
-static gpunmf_status generate_job_data(gpunmf_job *j, unsigned long long seed, float sigma) {
-    cudaStream_t s = j->stream;
-    const long long nr = (long long)j->n * j->r, rm = (long long)j->r * j->m, nm = (long long)j->n * j->m;
-    gen_uniform_kernel<<<gen_blocks(nr), 256, 0, s>>>(j->W, nr, stream_key(seed, 0), 0.f);   // A
-    gen_uniform_kernel<<<gen_blocks(rm), 256, 0, s>>>(j->H, rm, stream_key(seed, 1), 0.f);   // B
+// V (n x m), W (n x r), H (r x m) of a job with this seed, on stream s (W and H hold A and B while
+// V = A B is formed)
+static gpunmf_status generate_data(int n, int m, int r, unsigned long long seed, float sigma, float *V, float *W,
+                                   float *H, cudaStream_t s) {
+    const long long nr = (long long)n * r, rm = (long long)r * m, nm = (long long)n * m;
+    gen_uniform_kernel<<<gen_blocks(nr), 256, 0, s>>>(W, nr, stream_key(seed, 0), 0.f);   // A
+    gen_uniform_kernel<<<gen_blocks(rm), 256, 0, s>>>(H, rm, stream_key(seed, 1), 0.f);   // B
     GPUNMF_CUDA_TRY(cudaGetLastError());
-    GPUNMF_CUDA_TRY(gemm_f32(j->n, j->m, j->r, {j->W, j->n, false}, {j->H, j->r, false}, j->V, j->n, 1, s));
-    add_abs_noise_kernel<<<gen_blocks(nm), 256, 0, s>>>(j->V, nm, stream_key(seed, 2), sigma);
-    gen_uniform_kernel<<<gen_blocks(nr), 256, 0, s>>>(j->W, nr, stream_key(seed, 3), 1e-4f);
-    gen_uniform_kernel<<<gen_blocks(rm), 256, 0, s>>>(j->H, rm, stream_key(seed, 4), 1e-4f);
+    GPUNMF_CUDA_TRY(gemm_f32(n, m, r, {W, n, false}, {H, r, false}, V, n, 1, s));
+    add_abs_noise_kernel<<<gen_blocks(nm), 256, 0, s>>>(V, nm, stream_key(seed, 2), sigma);
+    gen_uniform_kernel<<<gen_blocks(nr), 256, 0, s>>>(W, nr, stream_key(seed, 3), 1e-4f);
+    gen_uniform_kernel<<<gen_blocks(rm), 256, 0, s>>>(H, rm, stream_key(seed, 4), 1e-4f);
     GPUNMF_CUDA_TRY(cudaGetLastError());
     return GPUNMF_OK;
+}
+
+// fills j->V, j->W, j->H on the job's stream
+static gpunmf_status generate_job_data(gpunmf_job *j, unsigned long long seed, float sigma) {
+    return generate_data(j->n, j->m, j->r, seed, sigma, j->V, j->W, j->H, j->stream);
 }
 
 }  // namespace gpunmf
@@ -146,11 +152,11 @@ static gpunmf_status capture_chunk(gpunmf_server *S, SJob *q) {
     GPUNMF_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     gpunmf_status st = chunk_body(S, q, S->check_every);
     cudaError_t e = cudaStreamEndCapture(s, &g);
-    if (st != GPUNMF_OK) {
+    if (st != GPUNMF_OK || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
-        return st;
+        if (st != GPUNMF_OK) return st;
+        GPUNMF_CUDA_TRY(e);
     }
-    GPUNMF_CUDA_TRY(e);
     e = cudaGraphInstantiate(&q->chunk_graph, g, 0);
     cudaGraphDestroy(g);
     GPUNMF_CUDA_TRY(e);
@@ -433,6 +439,15 @@ gpunmf_status gpunmf_server_stats(gpunmf_server *S, long long *submitted, long l
 double gpunmf_server_clock(gpunmf_server *S) { return S ? S->now() : -1.0; }
 
 // Stop accepting jobs, cancel the pending ones (status REJECTED), finish the admitted ones, free everything.
+gpunmf_status gpunmf_server_generate(int n, int m, int r, unsigned long long seed, float sigma, float *dV,
+                                     float *dW, float *dH, void *stream) {
+    if (n <= 0 || m <= 0 || r <= 0 || !dV || !dW || !dH || !(sigma >= 0.f)) {
+        set_error("gpunmf_server_generate: invalid arguments");
+        return GPUNMF_ERR_INVALID;
+    }
+    return generate_data(n, m, r, seed, sigma, dV, dW, dH, (cudaStream_t)stream);
+}
+
 gpunmf_status gpunmf_server_destroy(gpunmf_server *S) {
     if (!S) return GPUNMF_ERR_INVALID;
     {

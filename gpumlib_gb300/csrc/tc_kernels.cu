@@ -31,6 +31,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
+#include <climits>
 #include <mutex>
 #include <vector>
 
@@ -59,6 +61,7 @@ struct SkParams {
     uint32_t tmem_cols;
     float *partials;
     int *err;
+    long long wait_limit;  // clock64() cycles a bounded wait may last before the kernel gives up
     // Gram reduction done by the epilogue warps: gram_out[e] = sum_z gram_partials[z*E + e]
     const float *gram_partials;
     float *gram_out;
@@ -88,9 +91,9 @@ struct SkParams {
 
 extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
 
-__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, int *err, int bit) {
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, int *err, int bit, long long limit) {
     int ok = 0;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err, bit) ? 1 : 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err, bit, limit) ? 1 : 0;
     ok = __shfl_sync(0xffffffffu, ok, 0);
     return ok != 0;
 }
@@ -315,7 +318,7 @@ __device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float
     wk_bar();  // the slice's Gram entries are written by both warps: one release publishes them
     if (wt == 0) {
         red_release_add(pr.red_cnt, 1);
-        sflag[2] = flag_wait_ge(pr.red_cnt, G, pr.err, kErrWaitGram) ? 1 : 0;
+        sflag[2] = flag_wait_ge(pr.red_cnt, G, pr.err, kErrWaitGram, pr.wait_limit) ? 1 : 0;
     }
     wk_bar();
     if (!sflag[2]) return;  // the error word is set: the tail is skipped
@@ -384,7 +387,8 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             if (t1 > t0) last1 = pr.tile_readers[t1] - 1;
             bool ok = true;
             for (int t = t0; t <= t1 && ok; t++)
-                ok = flag_wait_ge(pr.tile_cnt + t, pr.slot_ptr[t + 1] - pr.slot_ptr[t], err, kErrWaitTile);
+                ok = flag_wait_ge(pr.tile_cnt + t, pr.slot_ptr[t + 1] - pr.slot_ptr[t], err, kErrWaitTile,
+                                  pr.wait_limit);
             if (ok) {
                 rd0 = atomicAdd(pr.tile_rd + t0, 1);
                 if (t1 > t0) rd1 = atomicAdd(pr.tile_rd + t1, 1);
@@ -636,7 +640,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             phase = pre == p.stages ? 1u : 0u;
             for (long long b = lo + pre; b < hi; b++) {
                 const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
-                if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty)) break;
+                if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) break;
                 mbar_arrive_expect_tx(&full[stage], stageA + stageB);
                 // adjacent boxes along K: each row's bytes of the stage are requested back to back
                 for (int q = 0; q < p.bps; q++)
@@ -670,11 +674,11 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             for (long long b = lo; b < hi && ok;) {
                 const long long t = b / p.kblocks;
                 const long long e = min(hi, (t + 1) * p.kblocks);
-                if (!mbar_wait(&tempty[acc], aphase ^ 1, p.err, kErrWaitTmemEmpty)) break;
+                if (!mbar_wait(&tempty[acc], aphase ^ 1, p.err, kErrWaitTmemEmpty, p.wait_limit)) break;
                 tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(acc * p.npad);
                 for (long long bb = b; bb < e; bb++) {
-                    if (!mbar_wait(&full[stage], phase, p.err, kErrWaitFull)) {
+                    if (!mbar_wait(&full[stage], phase, p.err, kErrWaitFull, p.wait_limit)) {
                         ok = false;
                         break;
                     }
@@ -742,7 +746,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
         for (long long b = lo; b < hi;) {
             const long long t = b / p.kblocks;
             const long long e = min(hi, (t + 1) * p.kblocks);
-            const bool ok = warp_wait(&tfull[acc], aphase, p.err, kErrWaitTmemFull);
+            const bool ok = warp_wait(&tfull[acc], aphase, p.err, kErrWaitTmemFull, p.wait_limit);
             if constexpr (FNP > 0) {
                 if (epi_bar_or(!ok)) break;  // the fused epilogue's barriers need all four warps
             } else if (!ok) {
@@ -825,6 +829,7 @@ struct QParams {
     float eps;
     double *partial;  // [grid]
     int *err;
+    long long wait_limit;
     int *done;        // CTAs finished (the last one sums the partials and resets it)
     float *out;       // the quality (device)
     float *out_host;  // the job's pinned read-back word, written directly where the device can (else null)
@@ -910,7 +915,7 @@ __global__ void __launch_bounds__(kQThreads, 1)
             st = pre == p.stages ? 0 : pre;
             ph = pre == p.stages ? 1u : 0u;
             for (int t = blockIdx.x + pre * gridDim.x; t < T; t += gridDim.x) {
-                if (!mbar_wait(&empty[st], ph ^ 1, p.err, kErrWaitEmpty)) break;
+                if (!mbar_wait(&empty[st], ph ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) break;
                 mbar_arrive_expect_tx(&full[st], (uint32_t)stageBytes);
                 load_ab(t, st);
                 load_v(t, st);
@@ -937,8 +942,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
             int st = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             for (int t = blockIdx.x; t < T; t += gridDim.x) {
-                if (!mbar_wait(&tempty[acc], aph ^ 1, p.err, kErrWaitTmemEmpty)) break;
-                if (!mbar_wait(&full[st], ph, p.err, kErrWaitFull)) break;
+                if (!mbar_wait(&tempty[acc], aph ^ 1, p.err, kErrWaitTmemEmpty, p.wait_limit)) break;
+                if (!mbar_wait(&full[st], ph, p.err, kErrWaitFull, p.wait_limit)) break;
                 tc_fence_after();
                 const uint32_t a0 = smem_u32(sA(st)), b0 = smem_u32(sB(st));
                 for (int k16 = 0; k16 < p.npad / 16; k16++)
@@ -970,8 +975,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
         int st = 0, acc = 0;
         uint32_t ph = 0, aph = 0;
         for (int t = blockIdx.x; t < T; t += gridDim.x) {
-            if (!warp_wait(&tfull[acc], aph, p.err, kErrWaitTmemFull)) break;
-            if (!warp_wait(&full[st], ph, p.err, kErrWaitFull)) break;  // the V tile of this stage
+            if (!warp_wait(&tfull[acc], aph, p.err, kErrWaitTmemFull, p.wait_limit)) break;
+            if (!warp_wait(&full[st], ph, p.err, kErrWaitFull, p.wait_limit)) break;  // the V tile of this stage
             tc_fence_after();
             const __nv_bfloat16 *v = sV(st);
             const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kQTile + c0);
@@ -1370,6 +1375,7 @@ struct KlParams {
     float eps;
     float *partials;
     int *err;
+    long long wait_limit;
     const float *sum_partials;  // [count][npad] partial sums of the other factor
     float *sum_out;             // [npad]
     int sum_count;
@@ -1418,9 +1424,10 @@ __device__ __forceinline__ void kl_fused_tail(const KlParams &p, float *smem, in
         if (tid == 0) {
             last0 = p.tile_readers[t0] - 1;
             if (t1 > t0) last1 = p.tile_readers[t1] - 1;
-            bool ok = !first || flag_wait_ge(p.sum_cnt, G, p.err, kErrWaitTile);
+            bool ok = !first || flag_wait_ge(p.sum_cnt, G, p.err, kErrWaitTile, p.wait_limit);
             for (int t = t0; t <= t1 && ok; t++)
-                ok = flag_wait_ge(p.tile_cnt + t, p.slot_ptr[t + 1] - p.slot_ptr[t], p.err, kErrWaitTile);
+                ok = flag_wait_ge(p.tile_cnt + t, p.slot_ptr[t + 1] - p.slot_ptr[t], p.err, kErrWaitTile,
+                                  p.wait_limit);
             if (ok) {
                 rd0 = atomicAdd(p.tile_rd + t0, 1);
                 if (t1 > t0) rd1 = atomicAdd(p.tile_rd + t1, 1);
@@ -1650,7 +1657,7 @@ __global__ void __launch_bounds__(kKlThreads)
                 // the factor rows of this row tile (MMA1's A), once per segment, as an entry of the F
                 // ring (same size: nbox boxes of 128 rows x 64 columns); the MMA thread copies it
                 // into TMEM and frees the entry
-                if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty)) break;
+                if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) break;
                 mbar_arrive_expect_tx(&ffull[fi], (uint32_t)fBytes);
                 for (int q = 0; q < p.nbox; q++) tma_load_2d(sF(fi) + q * kKlFBox, &tmA1, q * 64, t * kTileM, &ffull[fi]);
                 armed_f |= 1u << fi;
@@ -1658,7 +1665,7 @@ __global__ void __launch_bounds__(kKlThreads)
                 ring_next(fi, fph, p.sf);
                 for (long long bb = b; bb < e; bb++) {
                     const int k0 = (int)(bb % p.kblocks) * kKlBlockK;
-                    if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty)) {
+                    if (!mbar_wait_sleep(&fempty[fi], fph ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) {
                         ok = false;
                         break;
                     }
@@ -1668,7 +1675,7 @@ __global__ void __launch_bounds__(kKlThreads)
                     par_f = (par_f & ~(1u << fi)) | (fph << fi);
                     ring_next(fi, fph, p.sf);
                     if (bb < lo + vpre) continue;  // its V is already on the way
-                    if (!mbar_wait_sleep(&vempty[vi], vph ^ 1, p.err, kErrWaitEmpty)) {
+                    if (!mbar_wait_sleep(&vempty[vi], vph ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) {
                         ok = false;
                         break;
                     }
@@ -1728,7 +1735,8 @@ __global__ void __launch_bounds__(kKlThreads)
             if (j2 < j1 && __all_sync(0xffffffffu, mbar_test(&rfull[d2], d2ph))) {
                 // the accumulator of a new segment: the previous segment's numerator drained
                 if (first2 && seg2 > 0 &&
-                    !__all_sync(0xffffffffu, mbar_wait(tempty, (uint32_t)((seg2 - 1) & 1), p.err, kErrWaitTmemEmpty)))
+                    !__all_sync(0xffffffffu, mbar_wait(tempty, (uint32_t)((seg2 - 1) & 1), p.err, kErrWaitTmemEmpty,
+                                                       p.wait_limit)))
                     break;
                 if (leader) {
                     tc_fence_after();
@@ -1811,7 +1819,7 @@ __global__ void __launch_bounds__(kKlThreads)
                 const long long now = __shfl_sync(0xffffffffu, clock64(), 0);
                 if (t_idle == 0) {
                     t_idle = now;
-                } else if (now - t_idle > kWaitLimitCycles) {
+                } else if (now - t_idle > p.wait_limit) {
                     if (leader) atomicOr(p.err, kErrWaitFull);
                     break;
                 }
@@ -1870,8 +1878,8 @@ __global__ void __launch_bounds__(kKlThreads)
             // every block by all 16 warps (a quarter of the rows and a quarter of the columns each):
             // the ratio's latency, on the MMA1 -> MMA2 -> F-release chain, stays short
             for (long long bb = b; bb < e; bb++) {
-                if (!mbar_wait_sleep(&d1full[di], dph, p.err, kErrWaitTmemFull) ||
-                    !mbar_wait_sleep(&vfull[vi], vph, p.err, kErrWaitFull)) {
+                if (!mbar_wait_sleep(&d1full[di], dph, p.err, kErrWaitTmemFull, p.wait_limit) ||
+                    !mbar_wait_sleep(&vfull[vi], vph, p.err, kErrWaitFull, p.wait_limit)) {
                     ok = false;
                     break;
                 }
@@ -1919,7 +1927,7 @@ __global__ void __launch_bounds__(kKlThreads)
             }
             // the 16 warps leave together (the drain below ends at a barrier of all of them)
             if (kl_epi_bar_or(!ok)) break;
-            if (kl_epi_bar_or(!mbar_wait_sleep(tfull, (uint32_t)(seg & 1), p.err, kErrWaitTmemFull))) break;
+            if (kl_epi_bar_or(!mbar_wait_sleep(tfull, (uint32_t)(seg & 1), p.err, kErrWaitTmemFull, p.wait_limit))) break;
             tc_fence_after();
             float *dst = p.partials + ((size_t)(blockIdx.x * p.max_seg + seg) * kTileM + row) * p.npad;
             for (int c = part * 16; c < NP; c += 64) {  // the four warps of a quarter take turns by 16 columns
@@ -2124,6 +2132,7 @@ struct TcState {
     int qgrid = 0, qsmem = 0;
     float *GP_w = nullptr, *GP_h = nullptr;   // per-CTA Gram partials of the update kernels
     int gp_w_count = 0, gp_h_count = 0;
+    int max_ctas = 0;                         // CTAs per launch: the SMs, or fewer (gpunmf_set_grid_limit)
 };
 
 namespace gpunmf {
@@ -2162,6 +2171,9 @@ static gpunmf_status make_map(CUtensorMap *m, const void *base, uint64_t d0, uin
     }
     return GPUNMF_OK;
 }
+
+// CTAs per launch of the jobs created from now on (0: one per SM)
+static std::atomic<int> g_grid_limit{0};
 
 static int num_sms() {
     static int sms = 0;
@@ -2226,7 +2238,7 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     const int bps = (budget - 1280) / (2 * (kStageABytes + boxB)) >= 3 ? 2 : 1;
     const int kblocks = ceil_div(K, kBlockK * bps);
     const long long T = (long long)tiles * kblocks;
-    g.grid = (int)std::min<long long>(num_sms(), T);
+    g.grid = (int)std::min<long long>(j->tc->max_ctas, T);
     std::vector<int> ptr, list;
     int max_seg = 1;
     schedule(tiles, kblocks, g.grid, &max_seg, ptr, list);
@@ -2256,6 +2268,7 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     while (cols < (uint32_t)(2 * npad)) cols <<= 1;
     g.p.tmem_cols = cols;
     g.p.err = err;
+    g.p.wait_limit = kWaitLimitCycles;
     g.smem = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16 + (fnp ? 16 + fused_smem_bytes(fnp) : 0);
     g.fnp = fnp;
     size_t slots = (size_t)g.grid * max_seg;
@@ -2310,13 +2323,13 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
 
 // Largest number of stream-K segments on one tile for this GEMM shape (the fused update reads at
 // most kFusedSlots per tile); mirrors setup_gemm's schedule.
-static int schedule_max_slots(int rows, int K, int npad, int fnp) {
+static int schedule_max_slots(int rows, int K, int npad, int fnp, int max_ctas) {
     const int tiles = ceil_div(rows, kTileM);
     const int boxB = npad * kBlockK * 2;
     const int budget = fnp ? smem_optin() - fused_smem_bytes(fnp) - 64 : kSmemBudget;
     const int bps = (budget - 1280) / (2 * (kStageABytes + boxB)) >= 3 ? 2 : 1;
     const int kblocks = ceil_div(K, kBlockK * bps);
-    const int grid = (int)std::min<long long>(num_sms(), (long long)tiles * kblocks);
+    const int grid = (int)std::min<long long>(max_ctas, (long long)tiles * kblocks);
     std::vector<int> ptr, list;
     int max_seg = 1;
     schedule(tiles, kblocks, grid, &max_seg, ptr, list);
@@ -2515,7 +2528,7 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
     const int tiles = ceil_div(rows, kTileM);
     const int kblocks = ceil_div(K, kKlBlockK);
     const long long T = (long long)tiles * kblocks;
-    g.grid = (int)std::min<long long>(num_sms(), T);
+    g.grid = (int)std::min<long long>(j->tc->max_ctas, T);
     std::vector<int> ptr, list;
     int max_seg = 1;
     schedule(tiles, kblocks, g.grid, &max_seg, ptr, list);
@@ -2552,6 +2565,7 @@ static gpunmf_status setup_kl(gpunmf_job *j, KlGemm &g, int rows, int K, int npa
     g.p.nb = std::min(kKlMaxNB, (512 - npad - 64) / kKlBlockK);  // S/R buffers beside the accumulator and A1
     g.p.eps = j->eps;
     g.p.err = err;
+    g.p.wait_limit = kWaitLimitCycles;
     g.smem = fixed + sv * kKlVBytes + sf * fbytes;
     size_t slots = (size_t)g.grid * max_seg;
     cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
@@ -2763,6 +2777,7 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
     q.npad = t->npad;
     q.eps = j->eps;
     q.err = t->err;
+    q.wait_limit = kWaitLimitCycles;
     q.out = j->d_quality;
     {
         cudaError_t e = job_dev_alloc(j, (void **)&q.done, sizeof(int));
@@ -2780,7 +2795,7 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
     const int stageBytes = 4 * t->npad * 128 + kQVBytes;
     q.stages = std::min(3, (smem_optin() - 1024 - 256) / stageBytes);
     t->qsmem = 1024 + q.stages * stageBytes + (2 * q.stages + 5) * 8 + 8 + 2 * kQEpiWarps * 8 + 16;
-    t->qgrid = (int)std::min<long long>(num_sms(), (long long)q.tiles_i * q.tiles_u);
+    t->qgrid = (int)std::min<long long>(t->max_ctas, (long long)q.tiles_i * q.tiles_u);
     if (q.stages < 2 || (size_t)t->qgrid > j->red_cap) return GPUNMF_OK;  // not worth it here
     // Wb: {i, a}, Hb: {u, a}; boxes of 64 (contiguous) x npad (K rows; rows past r read zeros)
     gpunmf_status st = make_map(&t->tmQA, t->Wb, n, r, t->ldw, t->npad);
@@ -2862,6 +2877,10 @@ gpunmf_status tc_create(gpunmf_job *j) {
     j->tc = t;
     const int n = j->n, m = j->m, r = j->r;
     t->npad = npad_of(r);
+    {
+        const int cap = g_grid_limit.load();
+        t->max_ctas = std::min(num_sms(), cap > 0 ? cap : INT_MAX);
+    }
     t->ldv = ceil8(n);
     t->ldvt = ceil8(m);
     t->ldw = ceil8(n);
@@ -2886,7 +2905,8 @@ gpunmf_status tc_create(gpunmf_job *j) {
         return GPUNMF_ERR_NOMEM;
     }
     int fnp = fused_rank(t->npad);
-    if (fnp && (schedule_max_slots(m, n, t->npad, fnp) > kFusedSlots || schedule_max_slots(n, m, t->npad, fnp) > kFusedSlots))
+    if (fnp && (schedule_max_slots(m, n, t->npad, fnp, t->max_ctas) > kFusedSlots ||
+                schedule_max_slots(n, m, t->npad, fnp, t->max_ctas) > kFusedSlots))
         fnp = 0;
     gpunmf_status st = setup_gemm(j, t->gh, m, n, t->npad, &t->P_h, t->err, fnp);
     if (st == GPUNMF_OK) st = setup_gemm(j, t->gw, n, m, t->npad, &t->P_w, t->err, fnp);
@@ -3078,6 +3098,38 @@ gpunmf_status tc_check(gpunmf_job *j) {
     }
     return GPUNMF_OK;
 }
+
+void tc_set_wait_limit(gpunmf_job *j, long long cycles) {
+    TcState *t = j->tc;
+    if (!t) return;
+    const long long c = cycles > 0 ? cycles : kWaitLimitCycles;
+    t->gh.p.wait_limit = t->gw.p.wait_limit = c;
+    t->kh.p.wait_limit = t->kw.p.wait_limit = c;
+    t->qp.wait_limit = c;
+}
+
+// Host-side fault injection: the arrival counter of the first row tile of the next H-step (the
+// W-step where the rule has no H step) starts at -1 instead of 0, so after every partial product of
+// that tile has arrived it stands one below the count the fused update waits for.  The wait runs
+// out (bounded), the kernel sets the error word, the grid returns, and the host reports
+// GPUNMF_ERR_TIMEOUT.  Only jobs whose updates are fused into the product kernels have the counter.
+gpunmf_status tc_inject_missing_arrival(gpunmf_job *j) {
+    TcState *t = j->tc;
+    int *cnt = nullptr;
+    if (t && rule_is_kl(j->rule)) {
+        if (t->kh.p.X) cnt = t->kh.counters;
+    } else if (t && t->gh.fnp) {
+        cnt = j->rule == GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H ? t->gw.counters : t->gh.counters;
+    }
+    if (!cnt) {
+        set_error("this job has no fused update (no tile arrival counters)");
+        return GPUNMF_ERR_UNSUPPORTED;
+    }
+    GPUNMF_CUDA_TRY(cudaMemsetAsync(cnt, 0xFF, sizeof(int), j->stream));  // tile 0's count = -1
+    return GPUNMF_OK;
+}
+
+void tc_set_grid_limit(int ctas) { g_grid_limit.store(ctas > 0 ? ctas : 0); }
 
 void tc_destroy(gpunmf_job *j) {
     TcState *t = j->tc;

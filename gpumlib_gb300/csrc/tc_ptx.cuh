@@ -2,9 +2,10 @@
 // tcgen05 (TMEM alloc, MMA, commit, ld) and the shared-memory / instruction
 // descriptors of tcgen05.mma kind::f16.
 //
-// Every wait on an mbarrier is bounded: after kWaitLimitCycles of clock64()
-// it gives up, sets *err (global error word) and returns false, so a kernel
-// that misses an arrival ends with an error status instead of hanging.
+// Every wait on an mbarrier is bounded: after a limit of clock64() cycles
+// (kWaitLimitCycles unless the kernel's parameters carry another) it gives up,
+// sets *err (global error word) and returns false, so a kernel that misses an
+// arrival ends with an error status instead of hanging.
 #pragma once
 
 #include <cuda.h>
@@ -74,14 +75,15 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
 
 // Bounded wait for the phase with the given parity.  Returns false (and sets
 // err_bit in *err) if the limit is reached or another thread already failed.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int err_bit) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int err_bit,
+                                          long long limit = kWaitLimitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
     for (int spin = 0;; spin++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((spin & 255) == 255) {
             if (*((volatile int *)err) != 0) return false;
-            if (clock64() - t0 > kWaitLimitCycles) {
+            if (clock64() - t0 > limit) {
                 atomicOr(err, err_bit);
                 return false;
             }
@@ -103,14 +105,15 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t pari
 
 // Bounded wait that sleeps in the barrier instead of spinning, so waiting warps leave the issue
 // slots to the working ones.  Every lane of a warp may call it (uniform, no divergence).
-__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity, int *err, int err_bit) {
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity, int *err, int err_bit,
+                                                long long limit = kWaitLimitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     for (int spin = 0;; spin++) {
         if (mbar_try_wait_sleep(bar, parity, 20000u)) return true;
         if ((spin & 15) == 15) {
             if (*((volatile int *)err) != 0) return false;
-            if (clock64() - t0 > kWaitLimitCycles) {
+            if (clock64() - t0 > limit) {
                 atomicOr(err, err_bit);
                 return false;
             }
@@ -146,14 +149,15 @@ __device__ __forceinline__ int atom_acq_rel_add(int *addr, int v) {
 // Returns false (and sets err_bit in *err) on timeout or if another thread already failed.
 // The load is an acquire at GPU scope: after it and a barrier, the CTA's threads see what the
 // releases it observed published.
-__device__ __forceinline__ bool flag_wait_ge(const int *addr, int target, int *err, int err_bit) {
+__device__ __forceinline__ bool flag_wait_ge(const int *addr, int target, int *err, int err_bit,
+                                             long long limit = kWaitLimitCycles) {
     const long long t0 = clock64();
     for (;;) {
         int v;
         asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(addr) : "memory");
         if (v >= target) return true;
         if (*((volatile int *)err) != 0) return false;
-        if (clock64() - t0 > kWaitLimitCycles) {
+        if (clock64() - t0 > limit) {
             atomicOr(err, err_bit);
             return false;
         }

@@ -158,13 +158,37 @@ def serving_trace(rate=2000.0, duration=60.0, seed=7, lo=64, hi=4096, rmin=8, rm
     return jobs
 
 
+def _stream_key(seed, stream):
+    """Key of stream `stream` of a served job's seed: the counter generator's key with the stream
+    number in its top byte (the device generator's key schedule)."""
+    return np.uint64(int(_key(seed)) ^ (int(stream) << 56))
+
+
+def _uniform_key(key, count):
+    z = np.arange(1, int(count) + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = key + z * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(40)).astype(np.float32) * _SCALE
+
+
 def serving_job_data(job, noise_sd=0.01):
-    """V = A B + |N(0, noise_sd)| with A n x r, B r x m ~ U[0,1) (job seed); W, H U[0,1)+1e-4."""
-    g = np.random.Generator(np.random.PCG64(job["seed"]))
-    n, m, r = job["n"], job["m"], job["r"]
-    A = g.random((n, r), dtype=np.float32)
-    B = g.random((r, m), dtype=np.float32)
-    V = np.asfortranarray(A @ B + np.abs(g.normal(0.0, noise_sd, size=(n, m))).astype(np.float32))
-    W = np.asfortranarray(g.random((n, r), dtype=np.float32) + np.float32(1e-4))
-    H = np.asfortranarray(g.random((r, m), dtype=np.float32) + np.float32(1e-4))
+    """Host twin of the served jobs' device generator: V = A B + |N(0, noise_sd)| with A n x r and
+    B r x m uniform[0,1) (streams 0 and 1 of the job seed), the noise by Box-Muller from stream 2
+    (element k from uniforms 2k and 2k+1, the first shifted by half a step off zero); W, H
+    uniform[0,1) + 1e-4 (streams 3 and 4).  The uniforms are the same bits as on the device; V
+    differs from the device's only by float rounding (the product's summation order, log/cos).
+    Returns float32 column-major (V, W, H)."""
+    n, m, r, seed = job["n"], job["m"], job["r"], job["seed"]
+    A = colmajor(_uniform_key(_stream_key(seed, 0), n * r), n, r)
+    B = colmajor(_uniform_key(_stream_key(seed, 1), r * m), r, m)
+    u = _uniform_key(_stream_key(seed, 2), 2 * n * m).astype(np.float64)
+    u1, u2 = u[0::2] + 0.5 / 16777216.0, u[1::2]
+    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+    noise = colmajor(np.abs(noise_sd * z).astype(np.float32), n, m)
+    V = np.asfortranarray((A.astype(np.float64) @ B.astype(np.float64)).astype(np.float32) + noise)
+    W = colmajor(_uniform_key(_stream_key(seed, 3), n * r) + np.float32(1e-4), n, r)
+    H = colmajor(_uniform_key(_stream_key(seed, 4), r * m) + np.float32(1e-4), r, m)
     return V, W, H

@@ -126,6 +126,36 @@ gpunmf_status gpunmf_iterate(gpunmf_handle h, int iters, int updateW);
  */
 gpunmf_status gpunmf_set_quality_interval(gpunmf_handle h, int interval);
 
+/*
+ * Bounded device waits (no counterpart in the reference, whose kernels never
+ * wait on one another).  The BF16 kernels' CTAs wait on one another (tile
+ * arrivals, grid-wide sums); every such wait gives up after a limit of SM
+ * clock cycles, sets the job's error word, and the next call that reads it
+ * (synchronize, get, residual) returns GPUNMF_ERR_TIMEOUT; the job must then be
+ * destroyed.  Default limit: 4e9 cycles (about 2 s at 2 GHz); cycles <= 0
+ * restores it.  Applies to the job's later launches.  BF16 jobs only.
+ */
+gpunmf_status gpunmf_set_wait_limit_cycles(gpunmf_handle h, long long cycles);
+
+/*
+ * Host-side fault injection for tests of the path above: the arrival counter
+ * of the first row tile of the job's next fused half-step starts one below
+ * zero, so the fused update's wait for that tile cannot complete and runs out
+ * (bounded).  No GPU fault: the kernel returns with its error word set.
+ * GPUNMF_ERR_UNSUPPORTED for jobs without a fused update.
+ */
+gpunmf_status gpunmf_inject_missing_arrival(gpunmf_handle h);
+
+/*
+ * CTAs per launch of the tensor-core kernels of jobs created after this call
+ * (0 = one per SM, the default).  The fused kernels need their whole grid
+ * resident at once; an application that keeps long-running kernels of its own
+ * on some SMs (persistent kernels of another library, on other streams) caps
+ * the grid below the SMs those leave free, so the fused grid never waits for
+ * SMs that do not come free.  Process-wide.
+ */
+gpunmf_status gpunmf_set_grid_limit(int ctas);
+
 /* QualityImprovement() (nmf_base.h:148-150): lagged change of the quality; 1.0 initially. */
 gpunmf_status gpunmf_quality_improvement(gpunmf_handle h, float *out);
 
@@ -145,7 +175,9 @@ gpunmf_status gpunmf_residual_fp64(gpunmf_handle h, double *out);
  * product, at most 65536 CTAs; larger shapes are rejected with
  * GPUNMF_ERR_INVALID.  All calls share that array: calls that overlap on the
  * GPU race.  The first call on each device looks up the array's address;
- * make it before any stream capture begins.
+ * make it before any stream capture begins.  The address is kept for the
+ * life of the process: do not call this on a device after cudaDeviceReset()
+ * on that device.
  */
 gpunmf_status gpunmf_residual_fp64_noalloc(int n, int m, int r, const float *dV, const float *dW,
                                            const float *dH, double *dResult, void *stream);
@@ -301,6 +333,11 @@ gpunmf_status gpunmf_server_stats(gpunmf_server *s, long long *submitted, long l
 double gpunmf_server_clock(gpunmf_server *s);
 /* Cancels pending jobs, finishes admitted ones, frees everything. */
 gpunmf_status gpunmf_server_destroy(gpunmf_server *s);
+/* The data a served job with this seed starts from, written by the same device code into caller
+ * DEVICE buffers (V n x m, W n x r, H r x m; sigma 0.01 as the server uses), on `stream`: lets a
+ * caller rebuild a served job's inputs, e.g. to check its result against another implementation. */
+gpunmf_status gpunmf_server_generate(int n, int m, int r, unsigned long long seed, float sigma, float *dV,
+                                     float *dW, float *dH, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Kernel API: same names and arguments as src/cuda/nmf/nmf_kernels.h. */

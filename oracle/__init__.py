@@ -68,13 +68,21 @@ def _f32(a):
     return np.asfortranarray(np.asarray(a, dtype=np.float32)).copy(order="F")
 
 
+def _f32_in(a):
+    """A read-only operand (V): used as is when already float32 column-major, else converted."""
+    a = np.asarray(a)
+    if a.dtype == np.float32 and a.flags.f_contiguous:
+        return a
+    return np.asfortranarray(a, dtype=np.float32)
+
+
 def hostnmf_run(rule, V, W, H, iters, updateW=True, eps=1e-8, clamp_sums=False, nthreads=1,
                 residuals=False, skip_h=False):
     """Float transcription of HostNMF; rule 0 multiplicative Euclidean, 1 multiplicative KL,
     2 additive Euclidean (skip_h: the GPU class's H step that leaves H unchanged), 3 additive KL.
     Returns (W, H[, resid])."""
     lib = orc()
-    V = _f32(V); W = _f32(W); H = _f32(H)
+    V = _f32_in(V); W = _f32(W); H = _f32(H)
     n, m = V.shape
     r = W.shape[1]
     if rule in (0, 2):
@@ -117,6 +125,46 @@ def f64_run(rule, V, W, H, iters, updateW=True, eps=1e-8, nthreads=1):
             if lib.orc_f64_md_iter(n, m, r, _p(V), _p(W), _p(H), int(updateW), eps, _p(ws), nthreads) != 0:
                 raise ValueError("r too large for the oracle")
     return W, H
+
+
+def f64_run_blas(rule, V, W, H, iters, updateW=True, eps=1e-8):
+    """The same FP64 rules as f64_run with the products formed by numpy's BLAS (any summation order;
+    in FP64 that moves results by ~1e-13, far below what they check).  Used where f64_run's loops
+    would take minutes: full-size accuracy checks.
+      Euclidean (nmf_multiplicative_euclidian.cpp:29-67, nmf_kernels.cu:43-47):
+        H *= W'V / (W'W H + eps);  W *= V H' / (W H H' + eps)
+      KL (nmf_multiplicative_divergence.cpp:29-50, nmf_kernels.cu:63-233,247-341):
+        H *= W'(V / (W H + eps)) / max(colsum W, eps);  W *= (V / (W H + eps)) H' / max(rowsum H, eps)
+    Returns float64 (W, H)."""
+    V = np.asarray(V, dtype=np.float64)
+    W = np.array(W, dtype=np.float64)
+    H = np.array(H, dtype=np.float64)
+    for _ in range(iters):
+        if rule == 0:
+            H *= (W.T @ V) / ((W.T @ W) @ H + eps)
+            if updateW:
+                W *= (V @ H.T) / (W @ (H @ H.T) + eps)
+        elif rule == 1:
+            R = V / (W @ H + eps)
+            H *= (W.T @ R) / np.maximum(W.sum(axis=0), eps)[:, None]
+            if updateW:
+                R = V / (W @ H + eps)
+                W *= (R @ H.T) / np.maximum(H.sum(axis=1), eps)[None, :]
+            del R
+        else:
+            raise ValueError("rule %d has no FP64 restatement" % rule)
+    return W, H
+
+
+def factor_errors(Wg, Hg, Wd, Hd):
+    """Relative Frobenius errors of W, H and W H against a reference (W H formed in FP64)."""
+    def rel(a, b):
+        a = np.asarray(a, dtype=np.float64)
+        b = np.asarray(b, dtype=np.float64)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    Wg = np.asarray(Wg, dtype=np.float64)
+    Hg = np.asarray(Hg, dtype=np.float64)
+    return {"W": rel(Wg, Wd), "H": rel(Hg, Hd), "WH": rel(Wg @ Hg, Wd @ Hd)}
 
 
 def hostnmf_wh(W, H, nthreads=1):

@@ -191,3 +191,33 @@ def test_pool_reuse_and_trim(gpu):
             outs.append((nmf.GetW(), nmf.GetH()))
     for Wk, Hk in outs[1:]:
         assert np.array_equal(Wk, outs[0][0]) and np.array_equal(Hk, outs[0][1])
+
+
+def _slice_index(total, seed, edge=256, inner=256):
+    """Rows (or columns) to check: the first and last `edge`, and `inner` drawn from the rest (sorted),
+    so whole 128-row tiles at both ends and tiles split between stream-K segments are covered."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    mid = np.sort(g.choice(np.arange(edge, total - edge), size=inner, replace=False))
+    return np.r_[np.arange(edge), mid, np.arange(total - edge, total)]
+
+
+def test_headline_shape_one_iteration_matches_emulation(gpu):
+    """The benchmark workload itself (V 8192 x 8192 = A B + |N(0,0.01)|, r = 64, eps 1e-9): one BF16
+    iteration (two launches of the fused half-step kernel) against the exact emulation, evaluated on
+    768 columns of H and 768 rows of W -- the emulated FP64 products of the whole matrices would take
+    minutes on the host.  Same bound as the other shapes: 2e-5 relative Frobenius."""
+    cfg = inputs.large_euclidean(8192, 8192, 64)
+    V, W, H, eps = cfg["V"], cfg["W"], cfg["H"], np.float32(cfg["eps"])
+    with gpu.NMF_MultiplicativeEuclidianDistance(V, W, H, eps=eps, precision="bf16", quality_interval=0) as nmf:
+        nmf.DoIteration()
+        W1g, H1g = nmf.GetW(), nmf.GetH()
+    e = float(eps)
+    cols = _slice_index(8192, 1)
+    rows = _slice_index(8192, 2)
+    Wb = bf16(W)
+    Wd, Hd = W.astype(np.float64), H.astype(np.float64)
+    H1 = Hd[:, cols] * (Wb.T @ bf16(V[:, cols])) / ((Wd.T @ Wd) @ Hd[:, cols] + e)
+    assert rel(H1g[:, cols], H1) <= 2e-5, "H-step (fused half-step kernel) differs at 8192^2 r=64"
+    Hg = H1g.astype(np.float64)
+    W1 = Wd[rows] * (bf16(V[rows, :]) @ bf16(H1g).T) / (Wd[rows] @ (Hg @ Hg.T) + e)
+    assert rel(W1g[rows], W1) <= 2e-5, "W-step (fused half-step kernel) differs at 8192^2 r=64"

@@ -111,3 +111,32 @@ def test_kl_bf16_update_w_false_and_deterministic(gpu):
             nmf.DoIteration(updateW=False)
             outs.append((nmf.GetW(), nmf.GetH()))
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_kl_headline_shape_one_iteration_matches_emulation(gpu):
+    """The KL benchmark workload itself (V 16384 x 4096 Poisson counts, r = 128, eps 1e-9): one BF16
+    iteration of the fused KL kernels against the exact emulation on 768 columns of H and 768 rows of
+    W (the emulated products of the whole matrices would take minutes on the host); bound 2e-5."""
+    from test_gpu_bf16 import _slice_index
+    cfg = inputs.kl_counts()
+    V, W, H, eps = cfg["V"], cfg["W"], cfg["H"], np.float32(cfg["eps"])
+    with gpu.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision="bf16", quality_interval=0) as nmf:
+        nmf.DoIteration()
+        W1g, H1g = nmf.GetW(), nmf.GetH()
+    e = float(eps)
+    n, m = V.shape
+    cols = _slice_index(m, 3)
+    rows = _slice_index(n, 4)
+    Wb, Hb = bf16(W), bf16(H)
+    Wd, Hd = W.astype(np.float64), H.astype(np.float64)
+    S = Wb @ Hb[:, cols]
+    R = bf16((bf16(V[:, cols]) / (S + e)).astype(np.float32))
+    sw = np.maximum(Wd.sum(axis=0), e)
+    H1 = Hd[:, cols] * (Wb.T @ R) / sw[:, None]
+    assert rel(H1g[:, cols], H1) <= 2e-5, "H-step (fused KL kernel) differs at 16384x4096 r=128"
+    H1b = bf16(H1g)
+    S2 = Wb[rows] @ H1b
+    R2 = bf16((bf16(V[rows, :]) / (S2 + e)).astype(np.float32))
+    sh = np.maximum(H1g.astype(np.float64).sum(axis=1), e)
+    W1 = Wd[rows] * (R2 @ H1b.T) / sh[None, :]
+    assert rel(W1g[rows], W1) <= 2e-5, "W-step (fused KL kernel) differs at 16384x4096 r=128"

@@ -96,3 +96,75 @@ def test_replay_trace_small(gpu):
     assert all(r["status"] == 0 for r in results)
     lat = serve.latency_summary(results, unfinished, makespan)
     assert lat["p99_s"] is not None and lat["p99_s"] >= lat["p50_s"] > 0
+
+
+def _served_inputs(lib, n, m, r, seed):
+    """The inputs a served job with this seed starts from, written by the server's own device code."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from gpumlib_gb300 import _native, inputs
+    dV = torch.empty(n * m, dtype=torch.float32, device="cuda")
+    dW = torch.empty(n * r, dtype=torch.float32, device="cuda")
+    dH = torch.empty(r * m, dtype=torch.float32, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    _native.check(lib.gpunmf_server_generate(n, m, r, seed, 0.01, p(dV), p(dW), p(dH), None))
+    torch.cuda.synchronize()
+    return (inputs.colmajor(dV.cpu().numpy(), n, m), inputs.colmajor(dW.cpu().numpy(), n, r),
+            inputs.colmajor(dH.cpu().numpy(), r, m))
+
+
+SERVED = [dict(id=1, rule=0, n=600, m=450, r=16, seed=31), dict(id=2, rule=1, n=350, m=700, r=12, seed=32),
+          dict(id=3, rule=0, n=1300, m=900, r=48, seed=33), dict(id=4, rule=1, n=900, m=1100, r=40, seed=34)]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_served_results_match_oracle(gpu, precision):
+    """Served jobs (Euclidean and KL, overlapping on the device) against the CPU oracle from the same
+    inputs, rebuilt by the server's generator (and checked against its host twin).  FP32: W H within
+    1e-4 of the reference HostNMF arithmetic after the served iteration count (the drop-in bound).
+    BF16: W H within 5e-3 of the FP64 oracle (the bound of the other BF16 tests).  Each result's
+    residual is the oracle's residual of the returned factors."""
+    import oracle
+    from gpumlib_gb300 import _native, inputs
+    lib = _native.load()
+    with serve.Server(slots=8, precision=precision, check_every=10, tol=1e-9, max_iters=60, keep_factors=True) as s:
+        for j in SERVED:
+            s.submit(j["id"], j["rule"], j["n"], j["m"], j["r"], j["seed"], 1e-9)
+        assert s.drain(300)
+        out = {j["id"]: s.fetch(j["id"], j["n"], j["m"], j["r"]) for j in SERVED}
+    for j in SERVED:
+        res, W, H = out[j["id"]]
+        assert res["status"] == 0 and res["iters"] == 60
+        V, W0, H0 = _served_inputs(lib, j["n"], j["m"], j["r"], j["seed"])
+        tV, tW, tH = inputs.serving_job_data(j)
+        assert np.array_equal(W0, tW) and np.array_equal(H0, tH) and rel(V, tV) <= 1e-6
+        if precision == "fp32":
+            Wo, Ho = oracle.hostnmf_run(j["rule"], V, W0, H0, res["iters"], eps=np.float32(1e-9), clamp_sums=True,
+                                        nthreads=8)
+            bound = 1e-4
+        else:
+            Wo, Ho = oracle.f64_run_blas(j["rule"], V, W0, H0, res["iters"], eps=1e-9)
+            bound = 5e-3
+        err = oracle.factor_errors(W, H, Wo, Ho)
+        assert err["WH"] <= bound, (j, err)
+        assert abs(res["residual"] - oracle.residual(V, W, H)) <= 1e-6 * max(1.0, res["residual"])
+
+
+def test_served_stop_rule_matches_oracle(gpu):
+    """The stop rule of the reference's training loop (FacesNMFDlg.cpp:658-681), with the residual as
+    the test: a served FP32 job retires at the first check (every 10 iterations) whose residual is at
+    or below tol, the check at which the oracle's trajectory first reaches it."""
+    import oracle
+    from gpumlib_gb300 import _native
+    lib = _native.load()
+    j = dict(id=9, rule=0, n=500, m=400, r=32, seed=41)
+    V, W0, H0 = _served_inputs(lib, j["n"], j["m"], j["r"], j["seed"])
+    _, _, traj = oracle.hostnmf_run(0, V, W0, H0, 200, eps=np.float32(1e-9), nthreads=8, residuals=True)
+    checks = traj[9::10]
+    tol = float(np.sqrt(checks[3] * checks[4]))  # between the 4th and 5th checks: reached at iteration 50
+    with serve.Server(slots=2, precision="fp32", check_every=10, tol=tol, max_iters=200, keep_factors=True) as s:
+        s.submit(j["id"], j["rule"], j["n"], j["m"], j["r"], j["seed"], 1e-9)
+        assert s.drain(120)
+        res, W, H = s.fetch(j["id"], j["n"], j["m"], j["r"])
+    assert res["status"] == 0 and res["iters"] == 50, (res, checks[:6], tol)
+    assert res["residual"] <= tol < checks[3]

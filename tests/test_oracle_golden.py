@@ -105,3 +105,16 @@ def test_oracle_grouped_layout_and_stop():
         assert d[0] == 1.0 and d[1] == 1.0    # no improvement before the third sample
         assert its[s] == len(d) and (d[-1] < 0.5 or its[s] == 400)
         assert all(x >= 0.5 for x in d[2:-1] if x != 1.0)
+
+
+def test_f64_blas_restatement_matches_f64_loops():
+    """The BLAS-backed FP64 rules (used for full-size error checks) agree with the FP64 loops."""
+    from gpumlib_gb300 import inputs
+    for rule, (n, m, r) in ((0, (130, 97, 9)), (1, (61, 150, 5))):
+        V = inputs.uniform_matrix(31 + rule, n, m, add=0.01)
+        W, H = inputs.factors(41 + rule, n, m, r)
+        for updateW in (True, False):
+            Wa, Ha = oracle.f64_run(rule, V, W, H, 4, updateW=updateW, eps=1e-9)
+            Wb, Hb = oracle.f64_run_blas(rule, V, W, H, 4, updateW=updateW, eps=1e-9)
+            err = oracle.factor_errors(Wb, Hb, Wa, Ha)
+            assert max(err.values()) < 1e-12, (rule, updateW, err)

@@ -5,14 +5,17 @@ fixed array inside the library, so it never calls cudaMalloc.  It is checked
 through the C ABI against the job-based gpunmf_residual_fp64 (the existing
 entry point, which allocates its workspaces at job creation) on two calls in
 a row: a larger shape first, then a smaller one, so the second call runs with
-the first call's partial sums still in the shared scratch array.  The bound is
-the 1e-5 used for residuals elsewhere in these tests.
+the first call's partial sums still in the shared scratch array.  Each result
+is also checked against the CPU oracle's residual (all in FP64), so the check
+does not rest on the two entry points sharing their reduction code.  The bound
+is the 1e-5 used for residuals elsewhere in these tests.
 """
 import ctypes
 
 import numpy as np
 import pytest
 
+import oracle
 from gpumlib_gb300 import _native, inputs
 
 pytestmark = pytest.mark.gpu
@@ -42,6 +45,7 @@ def test_noalloc_residual_matches_job_residual_twice(gpu):
         torch.cuda.synchronize()
         got = out.item()
         assert abs(got - expected) <= TOL, (n, m, r, got, expected)
+        assert abs(got - oracle.residual(V, W, H)) <= TOL, (n, m, r, got)
 
 
 def test_noalloc_rejects_shapes_beyond_its_scratch(gpu):
