@@ -1,8 +1,11 @@
 // BF16 tensor-core path (tcgen05 + TMA) of the Euclidean multiplicative update.
 //
 // Data layout in HBM (per job, beside the FP32 masters V, W, H):
-//   Vb   n x m  BF16, column-major, ld = ceil8(n)   (V itself: rows i contiguous)
-//   Vbt  m x n  BF16, column-major, ld = ceil8(m)   (V transposed: columns u contiguous)
+//   Vb   V as BF16 in 16 KB chunks: chunk (u / 128, i / 64) holds its 128 columns u, each with
+//        its 64 rows i contiguous (128 bytes) -- one TMA box, read as one contiguous burst
+//   Vbt  V' as BF16 in the same chunking with the roles of i and u swapped
+//   (both zero-padded to multiples of 128 in n and m; chunk (t, c) at (t * kb64 + c) * 16 KB,
+//   kb64 = the padded K extent / 64)
 //   Wb   n x r  BF16, column-major, ld = ceil8(n)
 //   Hb   r x m  BF16, row-major,    ld = ceil8(m)
 // V is fixed for the whole job, so both BF16 copies are made once; with
@@ -57,6 +60,7 @@ static inline int npad_of(int r) { return (r + 15) / 16 * 16; }
 
 struct SkParams {
     int tiles, kblocks, npad, stages, max_seg;
+    int kb64;  // 64-wide chunks of V per row tile along K (the tiled layout)
     int bps;  // 64-wide TMA boxes per stage along K (1 or 2): a stage block covers bps*64 of K
     uint32_t tmem_cols;
     float *partials;
@@ -625,7 +629,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
                 mbar_arrive_expect_tx(&full[i], stageA + stageB);
                 for (int q = 0; q < p.bps; q++)
-                    tma_load_2d(sA + i * stageA + q * kStageABytes, &tmA, (kb * p.bps + q) * kBlockK, t * kTileM,
+                    tma_load_3d(sA + i * stageA + q * kStageABytes, &tmA, 0, 0, t * p.kb64 + kb * p.bps + q,
                                 &full[i]);
             }
             griddep_wait();
@@ -644,8 +648,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 mbar_arrive_expect_tx(&full[stage], stageA + stageB);
                 // adjacent boxes along K: each row's bytes of the stage are requested back to back
                 for (int q = 0; q < p.bps; q++)
-                    tma_load_2d(sA + stage * stageA + q * kStageABytes, &tmA, (kb * p.bps + q) * kBlockK,
-                                t * kTileM, &full[stage]);
+                    tma_load_3d(sA + stage * stageA + q * kStageABytes, &tmA, 0, 0, t * p.kb64 + kb * p.bps + q,
+                                &full[stage]);
                 for (int q = 0; q < p.bps; q++)
                     tma_load_2d(sB + stage * stageB + q * boxB, &tmB, (kb * p.bps + q) * kBlockK, 0, &full[stage]);
                 armed[stage]++;
@@ -826,6 +830,7 @@ __device__ __forceinline__ float lg2_approx(float x) {
 
 struct QParams {
     int tiles_i, tiles_u, npad, stages;
+    int kb64;         // 64-wide chunks of V' per 128-row tile along u
     float eps;
     double *partial;  // [grid]
     int *err;
@@ -891,8 +896,8 @@ __global__ void __launch_bounds__(kQThreads, 1)
             auto load_v = [&](int t, int s2) {  // V' tile: rows i, 64 columns u per box
                 const int ti = t / p.tiles_u, tu = t % p.tiles_u;
                 for (int q = 0; q < 2; q++)
-                    tma_load_2d(const_cast<__nv_bfloat16 *>(sV(s2)) + q * (kQTile * 64), &tmV, tu * kQTile + q * 64,
-                                ti * kQTile, &full[s2]);
+                    tma_load_3d(const_cast<__nv_bfloat16 *>(sV(s2)) + q * (kQTile * 64), &tmV, 0, 0,
+                                ti * p.kb64 + 2 * tu + q, &full[s2]);
             };
             auto load_ab = [&](int t, int s2) {
                 const int ti = t / p.tiles_u, tu = t % p.tiles_u;
@@ -1075,21 +1080,34 @@ __global__ void __launch_bounds__(kQThreads, 1)
 // ------------------------------------------------------------------------
 // conversions
 // ------------------------------------------------------------------------
-// V (n x m FP32 column-major) -> Vb (ld ldv) and Vbt (= V^T, ld ldvt), 32x32 tiles through shared memory
-__global__ void convert_v_kernel(const float *__restrict__ V, int n, int m, __nv_bfloat16 *__restrict__ Vb,
-                                 long long ldv, __nv_bfloat16 *__restrict__ Vbt, long long ldvt) {
-    __shared__ float tile[32][33];
-    const int i0 = blockIdx.x * 32, u0 = blockIdx.y * 32;
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        int i = i0 + threadIdx.x, u = u0 + k;
-        float v = (i < n && u < m) ? V[(long long)u * n + i] : 0.f;
-        tile[k][threadIdx.x] = v;
-        if (i < n && u < m) Vb[(long long)u * ldv + i] = __float2bfloat16_rn(v);
+// V (n x m FP32 column-major) -> Vb and Vbt in the tiled layout (16 KB chunks of 128 rows x 64 K,
+// zero beyond n and m): one 64 x 64 block of (i, u) per CTA through shared memory; each warp writes
+// whole 128-byte chunk rows (32 threads x two BF16 values).  npr, mpr: n, m rounded up to 128.
+__global__ void __launch_bounds__(256) convert_v_kernel(const float *__restrict__ V, int n, int m, int npr, int mpr,
+                                                        __nv_bfloat16 *__restrict__ Vb, __nv_bfloat16 *__restrict__ Vbt) {
+    __shared__ float tile[64][65];
+    const int i0 = blockIdx.x * 64, u0 = blockIdx.y * 64;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;  // 8 warps
+    const long long kb64i = npr / 64, kb64u = mpr / 64;
+    // rows u of the block: 64 values of i each, read coalesced, written as one chunk row of Vb
+    for (int uu = w; uu < 64; uu += 8) {
+        const int u = u0 + uu, i = i0 + 2 * lane;
+        float a = 0.f, b = 0.f;
+        if (u < m) {
+            if (i < n) a = V[(long long)u * n + i];
+            if (i + 1 < n) b = V[(long long)u * n + i + 1];
+        }
+        tile[uu][2 * lane] = a;
+        tile[uu][2 * lane + 1] = b;
+        __nv_bfloat16 *dst = Vb + (((long long)(u >> 7) * kb64i + (i0 >> 6)) * 128 + (u & 127)) * 64 + 2 * lane;
+        *reinterpret_cast<__nv_bfloat162 *>(dst) = __floats2bfloat162_rn(a, b);
     }
     __syncthreads();
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        int u = u0 + threadIdx.x, i = i0 + k;
-        if (i < n && u < m) Vbt[(long long)i * ldvt + u] = __float2bfloat16_rn(tile[threadIdx.x][k]);
+    // rows i of the block: 64 values of u each, one chunk row of Vbt
+    for (int ii = w; ii < 64; ii += 8) {
+        const int i = i0 + ii;
+        __nv_bfloat16 *dst = Vbt + (((long long)(i >> 7) * kb64u + (u0 >> 6)) * 128 + (i & 127)) * 64 + 2 * lane;
+        *reinterpret_cast<__nv_bfloat162 *>(dst) = __floats2bfloat162_rn(tile[2 * lane][ii], tile[2 * lane + 1][ii]);
     }
 }
 
@@ -1371,6 +1389,7 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
 // ========================================================================
 struct KlParams {
     int tiles, kblocks, npad, max_seg, nbox;
+    int kb64;        // 64-wide chunks of V per row tile along K (the tiled layout)
     int sv, sf, nb;  // V ring stages, F ring stages, S/R buffers in TMEM
     float eps;
     float *partials;
@@ -1641,10 +1660,10 @@ __global__ void __launch_bounds__(kKlThreads)
             bool ok = true;
             const long long vpre = min((long long)p.sv, hi - lo);  // fresh V stages: no empty wait
             for (long long bb = lo; bb < lo + vpre; bb++) {
-                const int t = (int)(bb / p.kblocks), k0 = (int)(bb % p.kblocks) * kKlBlockK;
+                const int t = (int)(bb / p.kblocks), c0 = t * p.kb64 + (int)(bb % p.kblocks) * 2;
                 mbar_arrive_expect_tx(&vfull[vi], (uint32_t)kKlVBytes);
-                tma_load_2d(sV(vi), &tmV, k0, t * kTileM, &vfull[vi]);
-                tma_load_2d(sV(vi) + kKlVBytes / 2, &tmV, k0 + 64, t * kTileM, &vfull[vi]);
+                tma_load_3d(sV(vi), &tmV, 0, 0, c0, &vfull[vi]);
+                tma_load_3d(sV(vi) + kKlVBytes / 2, &tmV, 0, 0, c0 + 1, &vfull[vi]);
                 armed_v |= 1u << vi;
                 par_v = (par_v & ~(1u << vi)) | (vph << vi);
                 ring_next(vi, vph, p.sv);
@@ -1680,8 +1699,9 @@ __global__ void __launch_bounds__(kKlThreads)
                         break;
                     }
                     mbar_arrive_expect_tx(&vfull[vi], (uint32_t)kKlVBytes);
-                    tma_load_2d(sV(vi), &tmV, k0, t * kTileM, &vfull[vi]);
-                    tma_load_2d(sV(vi) + kKlVBytes / 2, &tmV, k0 + 64, t * kTileM, &vfull[vi]);
+                    const int c0 = t * p.kb64 + (int)(bb % p.kblocks) * 2;
+                    tma_load_3d(sV(vi), &tmV, 0, 0, c0, &vfull[vi]);
+                    tma_load_3d(sV(vi) + kKlVBytes / 2, &tmV, 0, 0, c0 + 1, &vfull[vi]);
                     armed_v |= 1u << vi;
                     par_v = (par_v & ~(1u << vi)) | (vph << vi);
                     ring_next(vi, vph, p.sv);
@@ -2120,7 +2140,8 @@ struct TcState {
     long long ldr = 0;
     KlGemm kh, kw;
     float *S_w = nullptr, *S_h = nullptr, *SP_w = nullptr, *SP_h = nullptr;
-    long long ldv = 0, ldvt = 0, ldw = 0, ldh = 0;
+    long long ldw = 0, ldh = 0;
+    int npr = 0, mpr = 0;  // n and m rounded up to 128: the extents of the tiled Vb / Vbt
     int npad = 16;
     TcGemm gh, gw;  // H-step (W'V) and W-step (VH')
     float *P_h = nullptr, *P_w = nullptr;
@@ -2174,6 +2195,28 @@ static gpunmf_status make_map(CUtensorMap *m, const void *base, uint64_t d0, uin
 
 // CTAs per launch of the jobs created from now on (0: one per SM)
 static std::atomic<int> g_grid_limit{0};
+
+// Tiled BF16 copy of V (Vb or Vbt): `chunks` 16 KB chunks of 128 rows x 64 K values, 128-byte rows;
+// box {64, 128, 1} = one chunk, 128B swizzle.
+static gpunmf_status make_map_tiled(CUtensorMap *m, const void *base, uint64_t chunks) {
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return GPUNMF_ERR_CUDA;
+    }
+    cuuint64_t dims[3] = {64, 128, chunks};
+    cuuint64_t strides[2] = {128, 128 * 128};
+    cuuint32_t box[3] = {64, 128, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (tiled V) failed (%d)", (int)r);
+        return GPUNMF_ERR_CUDA;
+    }
+    return GPUNMF_OK;
+}
 
 static int num_sms() {
     static int sms = 0;
@@ -2712,8 +2755,8 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
     const int n = j->n, m = j->m, r = j->r;
     t->ldr = t->npad;
     const int cw = ceil_div(n, kUpdCols), ch = ceil_div(m, kUpdCols);
-    cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->ldv * m * 2);
-    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->ldvt * n * 2);
+    cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->npr * t->mpr * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->npr * t->mpr * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hb, (size_t)t->ldh * r * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wr, (size_t)n * t->ldr * 2);
@@ -2754,11 +2797,13 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
         fuse(t->kw, j->W, t->Wb, t->ldw, t->Wr, n, 1, n, t->kh);
     }
     // H-step: rows u; V tile from Vb, A1 = Hc rows u, F = Wr rows i
-    st = make_map(&t->kh.tmV, t->Vb, n, m, t->ldv, kTileM);
+    st = make_map_tiled(&t->kh.tmV, t->Vb, (uint64_t)(t->mpr / 128) * (t->npr / 64));
+    t->kh.p.kb64 = t->npr / 64;
+    t->kw.p.kb64 = t->mpr / 64;
     if (st == GPUNMF_OK) st = make_map(&t->kh.tmA1, t->Hc, r, m, t->ldr, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->kh.tmF, t->Wr, r, n, t->ldr, kKlBlockK);
     // W-step: rows i; V tile from Vbt, A1 = Wr rows i, F = Hc rows u
-    if (st == GPUNMF_OK) st = make_map(&t->kw.tmV, t->Vbt, m, n, t->ldvt, kTileM);
+    if (st == GPUNMF_OK) st = make_map_tiled(&t->kw.tmV, t->Vbt, (uint64_t)(t->npr / 128) * (t->mpr / 64));
     if (st == GPUNMF_OK) st = make_map(&t->kw.tmA1, t->Wr, r, n, t->ldr, kTileM);
     if (st == GPUNMF_OK) st = make_map(&t->kw.tmF, t->Hc, r, m, t->ldr, kKlBlockK);
     if (st != GPUNMF_OK) return st;
@@ -2800,7 +2845,9 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
     // Wb: {i, a}, Hb: {u, a}; boxes of 64 (contiguous) x npad (K rows; rows past r read zeros)
     gpunmf_status st = make_map(&t->tmQA, t->Wb, n, r, t->ldw, t->npad);
     if (st == GPUNMF_OK) st = make_map(&t->tmQB, t->Hb, m, r, t->ldh, t->npad);
-    if (st == GPUNMF_OK) st = make_map(&t->tmQV, t->Vbt, m, n, t->ldvt, kQTile);  // V': {u, i}, box {64, 128}
+    // V': chunks of 128 rows i x 64 columns u
+    if (st == GPUNMF_OK) st = make_map_tiled(&t->tmQV, t->Vbt, (uint64_t)(t->npr / 128) * (t->mpr / 64));
+    q.kb64 = t->mpr / 64;
     if (st != GPUNMF_OK) return st;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
@@ -2858,13 +2905,14 @@ void tc_add_sizes(int, int, int, int, size_t *) {}
 size_t tc_footprint(int rule, int n, int m, int r) {
     const int npad = npad_of(r);
     if (rule_is_kl(rule)) {
-        size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r +
-                        (size_t)(n + m) * npad);
+        size_t b = 2 * (2 * (size_t)((n + 127) / 128 * 128) * ((m + 127) / 128 * 128) + (size_t)ceil8(n) * r +
+                        (size_t)ceil8(m) * r + (size_t)(n + m) * npad);
         b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
         b += (size_t)npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
         return b;
     }
-    size_t b = 2 * ((size_t)ceil8(n) * m + (size_t)ceil8(m) * n + (size_t)ceil8(n) * r + (size_t)ceil8(m) * r);
+    size_t b = 2 * (2 * (size_t)((n + 127) / 128 * 128) * ((m + 127) / 128 * 128) + (size_t)ceil8(n) * r +
+                    (size_t)ceil8(m) * r);
     b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
     b += (size_t)npad * npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
     b += fused_bytes(m, npad) + fused_bytes(n, npad);
@@ -2881,13 +2929,13 @@ gpunmf_status tc_create(gpunmf_job *j) {
         const int cap = g_grid_limit.load();
         t->max_ctas = std::min(num_sms(), cap > 0 ? cap : INT_MAX);
     }
-    t->ldv = ceil8(n);
-    t->ldvt = ceil8(m);
+    t->npr = (n + 127) / 128 * 128;
+    t->mpr = (m + 127) / 128 * 128;
     t->ldw = ceil8(n);
     t->ldh = ceil8(m);
     if (rule_is_kl(j->rule)) return tc_create_kl(j);
-    cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->ldv * m * 2);
-    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->ldvt * n * 2);
+    cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->npr * t->mpr * 2);
+    if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->npr * t->mpr * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Hb, (size_t)t->ldh * r * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->err, sizeof(int));
@@ -2935,10 +2983,12 @@ gpunmf_status tc_create(gpunmf_job *j) {
         t->gw.p.gram_entries = (int)rp2;
     }
     // H-step: rows = u (columns of V): A = Vb (dim0 i over n, dim1 u over m); B = Wb (dim0 i, dim1 a)
-    st = make_map(&t->gh.tmA, t->Vb, n, m, t->ldv, kTileM);
+    st = make_map_tiled(&t->gh.tmA, t->Vb, (uint64_t)(t->mpr / 128) * (t->npr / 64));
+    t->gh.p.kb64 = t->npr / 64;
+    t->gw.p.kb64 = t->mpr / 64;
     if (st == GPUNMF_OK) st = make_map(&t->gh.tmB, t->Wb, n, r, t->ldw, t->npad);
     // W-step: rows = i: A = Vbt (dim0 u over m, dim1 i over n); B = Hb (dim0 u, dim1 a)
-    if (st == GPUNMF_OK) st = make_map(&t->gw.tmA, t->Vbt, m, n, t->ldvt, kTileM);
+    if (st == GPUNMF_OK) st = make_map_tiled(&t->gw.tmA, t->Vbt, (uint64_t)(t->npr / 128) * (t->mpr / 64));
     if (st == GPUNMF_OK) st = make_map(&t->gw.tmB, t->Hb, m, r, t->ldh, t->npad);
     if (st != GPUNMF_OK) return st;
     // The attribute is per function, shared by every job in the process: set it once to the
@@ -2955,8 +3005,7 @@ gpunmf_status tc_create(gpunmf_job *j) {
 gpunmf_status tc_prepare(gpunmf_job *j) {
     TcState *t = j->tc;
     cudaStream_t s = j->stream;
-    dim3 grid(ceil_div(j->n, 32), ceil_div(j->m, 32));
-    convert_v_kernel<<<grid, dim3(32, 8), 0, s>>>(j->V, j->n, j->m, t->Vb, t->ldv, t->Vbt, t->ldvt);
+    convert_v_kernel<<<dim3(t->npr / 64, t->mpr / 64), 256, 0, s>>>(j->V, j->n, j->m, t->npr, t->mpr, t->Vb, t->Vbt);
     convert_w_kernel<<<std::min(1024, ceil_div((long long)j->n * j->r, 256)), 256, 0, s>>>(j->W, j->n, j->r,
                                                                                           t->Wb, t->ldw);
     convert_h_kernel<<<std::min(1024, ceil_div((long long)j->r * j->m, 256)), 256, 0, s>>>(j->H, j->r, j->m,
