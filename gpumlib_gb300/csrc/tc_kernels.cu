@@ -619,6 +619,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
 
     if (warp == 0) {
         if (lane == 0) {
+            const uint64_t vpol = l2_policy_evict_first();  // V is read once per launch
             int stage = 0;
             uint32_t phase = 0;
             int armed[kMaxStages];
@@ -629,8 +630,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
                 mbar_arrive_expect_tx(&full[i], stageA + stageB);
                 for (int q = 0; q < p.bps; q++)
-                    tma_load_3d(sA + i * stageA + q * kStageABytes, &tmA, 0, 0, t * p.kb64 + kb * p.bps + q,
-                                &full[i]);
+                    tma_load_3d_hint(sA + i * stageA + q * kStageABytes, &tmA, 0, 0, t * p.kb64 + kb * p.bps + q,
+                                     &full[i], vpol);
             }
             griddep_wait();
             griddep_launch_dependents();
@@ -648,8 +649,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 mbar_arrive_expect_tx(&full[stage], stageA + stageB);
                 // adjacent boxes along K: each row's bytes of the stage are requested back to back
                 for (int q = 0; q < p.bps; q++)
-                    tma_load_3d(sA + stage * stageA + q * kStageABytes, &tmA, 0, 0, t * p.kb64 + kb * p.bps + q,
-                                &full[stage]);
+                    tma_load_3d_hint(sA + stage * stageA + q * kStageABytes, &tmA, 0, 0, t * p.kb64 + kb * p.bps + q,
+                                     &full[stage], vpol);
                 for (int q = 0; q < p.bps; q++)
                     tma_load_2d(sB + stage * stageB + q * boxB, &tmB, (kb * p.bps + q) * kBlockK, 0, &full[stage]);
                 armed[stage]++;
@@ -893,11 +894,12 @@ __global__ void __launch_bounds__(kQThreads, 1)
             int st = 0;
             uint32_t ph = 0;
             int armed[4] = {0, 0, 0, 0};
+            const uint64_t vpol = l2_policy_evict_first();  // V is read once per sample
             auto load_v = [&](int t, int s2) {  // V' tile: rows i, 64 columns u per box
                 const int ti = t / p.tiles_u, tu = t % p.tiles_u;
                 for (int q = 0; q < 2; q++)
-                    tma_load_3d(const_cast<__nv_bfloat16 *>(sV(s2)) + q * (kQTile * 64), &tmV, 0, 0,
-                                ti * p.kb64 + 2 * tu + q, &full[s2]);
+                    tma_load_3d_hint(const_cast<__nv_bfloat16 *>(sV(s2)) + q * (kQTile * 64), &tmV, 0, 0,
+                                     ti * p.kb64 + 2 * tu + q, &full[s2], vpol);
             };
             auto load_ab = [&](int t, int s2) {
                 const int ti = t / p.tiles_u, tu = t % p.tiles_u;
@@ -1653,6 +1655,7 @@ __global__ void __launch_bounds__(kKlThreads)
 
     if (warp == 0) {
         if (lane == 0) {
+            const uint64_t vpol = l2_policy_evict_first();  // V is read once per launch
             int vi = 0, fi = 0, seg = 0;
             uint32_t vph = 0, fph = 0;
             // the last phase armed on each full barrier (bit set) and its parity, for the drain below
@@ -1662,8 +1665,8 @@ __global__ void __launch_bounds__(kKlThreads)
             for (long long bb = lo; bb < lo + vpre; bb++) {
                 const int t = (int)(bb / p.kblocks), c0 = t * p.kb64 + (int)(bb % p.kblocks) * 2;
                 mbar_arrive_expect_tx(&vfull[vi], (uint32_t)kKlVBytes);
-                tma_load_3d(sV(vi), &tmV, 0, 0, c0, &vfull[vi]);
-                tma_load_3d(sV(vi) + kKlVBytes / 2, &tmV, 0, 0, c0 + 1, &vfull[vi]);
+                tma_load_3d_hint(sV(vi), &tmV, 0, 0, c0, &vfull[vi], vpol);
+                tma_load_3d_hint(sV(vi) + kKlVBytes / 2, &tmV, 0, 0, c0 + 1, &vfull[vi], vpol);
                 armed_v |= 1u << vi;
                 par_v = (par_v & ~(1u << vi)) | (vph << vi);
                 ring_next(vi, vph, p.sv);
@@ -1700,8 +1703,8 @@ __global__ void __launch_bounds__(kKlThreads)
                     }
                     mbar_arrive_expect_tx(&vfull[vi], (uint32_t)kKlVBytes);
                     const int c0 = t * p.kb64 + (int)(bb % p.kblocks) * 2;
-                    tma_load_3d(sV(vi), &tmV, 0, 0, c0, &vfull[vi]);
-                    tma_load_3d(sV(vi) + kKlVBytes / 2, &tmV, 0, 0, c0 + 1, &vfull[vi]);
+                    tma_load_3d_hint(sV(vi), &tmV, 0, 0, c0, &vfull[vi], vpol);
+                    tma_load_3d_hint(sV(vi) + kKlVBytes / 2, &tmV, 0, 0, c0 + 1, &vfull[vi], vpol);
                     armed_v |= 1u << vi;
                     par_v = (par_v & ~(1u << vi)) | (vph << vi);
                     ring_next(vi, vph, p.sv);
