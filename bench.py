@@ -372,9 +372,13 @@ def run_ours(args, rank, world, local, dist):
            "config": workload_config(n, m, r, eps, world),
            "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roofline}
 
-    # end to end through the public API from pinned host buffers
+    # end to end through the public API from pinned host buffers: the workload's own job (the
+    # configuration's 500 iterations, --full-job-iters), and a job of --steps iterations beside it
     if not args.no_e2e:
-        out["e2e"] = run_e2e(lib, g, V, W, H, eps, precision, args, dist, world)
+        job_iters = args.full_job_iters or args.steps
+        out["e2e"] = run_e2e(lib, g, V, W, H, eps, precision, args, dist, world, iters=job_iters)
+        if job_iters != args.steps:
+            out["e2e_short_job"] = run_e2e(lib, g, V, W, H, eps, precision, args, dist, world)
 
     # equal-residual check: a full job in each precision, and the error of W, H and W H against the
     # FP64 oracle after a few iterations from the same start
@@ -451,8 +455,8 @@ def run_e2e(lib, g, V, W, H, eps, precision, args, dist, world, iters=None, make
         return {"value": round(world * steps / dt, 2), "unit": "iters/s",
                 "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps,
                 "note": "one job of %d iterations from pinned host buffers, after one untimed warm-up job: create "
-                        "(H2D V,W,H), iterations with quality read-back, GetW/GetH (D2H); bytes amortised per step"
-                        % steps}
+                        "(V, W, H read from the host), iterations with the per-iteration quality read-back, GetW/GetH "
+                        "(D2H); bytes amortised per step" % steps}
     finally:
         for p in bufs:
             lib.gpunmf_host_free(p)

@@ -85,7 +85,9 @@ gpunmf_status tc_supported(int rule, int n, int m, int r);
 void tc_add_sizes(int rule, int n, int m, int r, size_t *red_doubles);
 size_t tc_footprint(int rule, int n, int m, int r);
 gpunmf_status tc_create(gpunmf_job *j);
-gpunmf_status tc_prepare(gpunmf_job *j);  // after V/W/H are uploaded
+// after V/W/H are uploaded; or, with v_src (V in host memory the device can read), after W/H are:
+// then the BF16 conversion reads V from there and also writes the job's FP32 V
+gpunmf_status tc_prepare(gpunmf_job *j, const float *v_src = nullptr);
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW);
 // quality of the current factors on the tensor cores (BF16 jobs with npad <= 128)
 bool tc_quality_ready(const gpunmf_job *j);

@@ -95,9 +95,11 @@ struct SkParams {
 
 extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
 
+// Wait of a whole warp on an mbarrier phase: lane 0 waits suspended in the barrier (a spinning lane
+// would take issue slots from the warps that work meanwhile), the others at the shuffle.
 __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, int *err, int bit, long long limit) {
     int ok = 0;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err, bit, limit) ? 1 : 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait_sleep(bar, parity, err, bit, limit) ? 1 : 0;
     ok = __shfl_sync(0xffffffffu, ok, 0);
     return ok != 0;
 }
@@ -1085,30 +1087,41 @@ __global__ void __launch_bounds__(kQThreads, 1)
 // V (n x m FP32 column-major) -> Vb and Vbt in the tiled layout (16 KB chunks of 128 rows x 64 K,
 // zero beyond n and m): one 64 x 64 block of (i, u) per CTA through shared memory; each warp writes
 // whole 128-byte chunk rows (32 threads x two BF16 values).  npr, mpr: n, m rounded up to 128.
+// V may be host memory the device can read (the job's creation reads the caller's matrix once,
+// over the host link, instead of copying it first); then Vcopy receives the FP32 device copy.
 __global__ void __launch_bounds__(256) convert_v_kernel(const float *__restrict__ V, int n, int m, int npr, int mpr,
-                                                        __nv_bfloat16 *__restrict__ Vb, __nv_bfloat16 *__restrict__ Vbt) {
+                                                        __nv_bfloat16 *__restrict__ Vb, __nv_bfloat16 *__restrict__ Vbt,
+                                                        float *__restrict__ Vcopy) {
     __shared__ float tile[64][65];
     const int i0 = blockIdx.x * 64, u0 = blockIdx.y * 64;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;  // 8 warps
     const long long kb64i = npr / 64, kb64u = mpr / 64;
-    // rows u of the block: 64 values of i each, read coalesced, written as one chunk row of Vb
-    for (int uu = w; uu < 64; uu += 8) {
-        const int u = u0 + uu, i = i0 + 2 * lane;
-        float a = 0.f, b = 0.f;
-        if (u < m) {
-            if (i < n) a = V[(long long)u * n + i];
-            if (i + 1 < n) b = V[(long long)u * n + i + 1];
-        }
-        tile[uu][2 * lane] = a;
-        tile[uu][2 * lane + 1] = b;
+    const int i = i0 + 2 * lane;
+    // rows u of the block (8 per warp): 64 values of i each, all loads issued before any store
+    float a[8], b[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int u = u0 + w + 8 * q;
+        a[q] = (u < m && i < n) ? V[(long long)u * n + i] : 0.f;
+        b[q] = (u < m && i + 1 < n) ? V[(long long)u * n + i + 1] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int uu = w + 8 * q, u = u0 + uu;
+        tile[uu][2 * lane] = a[q];
+        tile[uu][2 * lane + 1] = b[q];
         __nv_bfloat16 *dst = Vb + (((long long)(u >> 7) * kb64i + (i0 >> 6)) * 128 + (u & 127)) * 64 + 2 * lane;
-        *reinterpret_cast<__nv_bfloat162 *>(dst) = __floats2bfloat162_rn(a, b);
+        *reinterpret_cast<__nv_bfloat162 *>(dst) = __floats2bfloat162_rn(a[q], b[q]);
+        if (Vcopy && u < m) {
+            if (i < n) Vcopy[(long long)u * n + i] = a[q];
+            if (i + 1 < n) Vcopy[(long long)u * n + i + 1] = b[q];
+        }
     }
     __syncthreads();
     // rows i of the block: 64 values of u each, one chunk row of Vbt
     for (int ii = w; ii < 64; ii += 8) {
-        const int i = i0 + ii;
-        __nv_bfloat16 *dst = Vbt + (((long long)(i >> 7) * kb64u + (u0 >> 6)) * 128 + (i & 127)) * 64 + 2 * lane;
+        const int ir = i0 + ii;
+        __nv_bfloat16 *dst = Vbt + (((long long)(ir >> 7) * kb64u + (u0 >> 6)) * 128 + (ir & 127)) * 64 + 2 * lane;
         *reinterpret_cast<__nv_bfloat162 *>(dst) = __floats2bfloat162_rn(tile[2 * lane][ii], tile[2 * lane + 1][ii]);
     }
 }
@@ -3005,10 +3018,12 @@ gpunmf_status tc_create(gpunmf_job *j) {
     return setup_quality(j);
 }
 
-gpunmf_status tc_prepare(gpunmf_job *j) {
+gpunmf_status tc_prepare(gpunmf_job *j, const float *v_src) {
     TcState *t = j->tc;
     cudaStream_t s = j->stream;
-    convert_v_kernel<<<dim3(t->npr / 64, t->mpr / 64), 256, 0, s>>>(j->V, j->n, j->m, t->npr, t->mpr, t->Vb, t->Vbt);
+    // from the job's V, or straight from the caller's matrix (which also fills the job's V)
+    convert_v_kernel<<<dim3(t->npr / 64, t->mpr / 64), 256, 0, s>>>(v_src ? v_src : j->V, j->n, j->m, t->npr, t->mpr,
+                                                                    t->Vb, t->Vbt, v_src ? j->V : nullptr);
     convert_w_kernel<<<std::min(1024, ceil_div((long long)j->n * j->r, 256)), 256, 0, s>>>(j->W, j->n, j->r,
                                                                                           t->Wb, t->ldw);
     convert_h_kernel<<<std::min(1024, ceil_div((long long)j->r * j->m, 256)), 256, 0, s>>>(j->H, j->r, j->m,
