@@ -341,6 +341,8 @@ static gpunmf_status quality_step(gpunmf_job *j, bool fused_wh) {
     j->q_last = quality;
     cudaStream_t s = j->stream;
     int n = j->n, m = j->m, r = j->r;
+    // BF16 jobs whose H-step can carry the sample: no launch of its own (the H-step records the event)
+    if (j->precision == GPUNMF_BF16 && tc_quality_fold(j)) return GPUNMF_OK;
     if (j->precision == GPUNMF_BF16 && tc_quality_ready(j)) {
         // BF16 jobs: W H on the tensor cores from the BF16 factors, V as BF16; one launch that also
         // writes the value into the pinned read-back word where the device can reach it

@@ -94,6 +94,9 @@ bool tc_quality_ready(const gpunmf_job *j);
 // whether the tensor-core quality kernel writes the job's pinned read-back word itself
 bool tc_quality_writes_host(const gpunmf_job *j);
 gpunmf_status tc_quality(gpunmf_job *j);
+// fused Euclidean jobs: the next H-step launch samples the quality itself (it also records the
+// job's quality event); false where it cannot
+bool tc_quality_fold(gpunmf_job *j);
 gpunmf_status tc_check(gpunmf_job *j);    // reads the kernels' error word (after a sync)
 void tc_set_wait_limit(gpunmf_job *j, long long cycles);  // <= 0: the default (about 2 s)
 gpunmf_status tc_inject_missing_arrival(gpunmf_job *j);

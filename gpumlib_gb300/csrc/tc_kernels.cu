@@ -91,6 +91,12 @@ struct SkParams {
     float *G_full;                     // npad^2: the complete Gram of the other factor, assembled here
     int *red_cnt;                      // [2]: Gram slices published, CTAs done reading (last resets)
     float *gp;                         // [grid][npad^2] this kernel's per-CTA partials of the new factor
+    // quality sample folded into an H-step (kernels with quality warps): sum V log10(WH + eps) - WH of
+    // the factors this launch starts from (nmf_kernels_quality.cu:35), WH formed block by block
+    float qeps;
+    double *qpartial;                  // [grid] per-CTA partials
+    int *qdone;                        // CTAs done (the last sums the partials in CTA order, resets it)
+    float *qout, *qout_host;           // the value: device word, and the pinned read-back word (or null)
 };
 
 extern __shared__ __align__(1024) unsigned char tc_dyn_smem[];
@@ -346,12 +352,20 @@ __device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float
 // until the chunk's tiles have all their partial products, sum them in K order,
 // X_new = X num / (den + eps) or max(0, X + X / den (num - den)), write X and its BF16 copy and
 // add the new rows to this CTA's Gram partial, which the next kernel sums with the other CTAs'.
-template <int NP>
+// barrier of the NT threads that run the fused tail: the whole CTA, or (SUBSET) its first NT
+// threads (named barrier 4)
+template <int NT, bool SUBSET>
+__device__ __forceinline__ void tail_sync() {
+    if constexpr (SUBSET) asm volatile("bar.sync 4, %0;" ::"n"(NT) : "memory");
+    else __syncthreads();
+}
+
+template <int NP, int NT = 256, bool SUBSET = false>
 __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *sG, float *sX, int *sflag, int *sSl) {
-    constexpr int NT = 256;
     using L = FusedLayout<NP, NT>;
     constexpr int E = NP * NP;
-    constexpr int GB = NP / 16;  // Gram partial: a GB x GB block per thread (16 x 16 threads)
+    // Gram partial: a GB x GB2 block per thread (16 x TB threads)
+    constexpr int TB = NT / 16, GB = NP / 16, GB2 = NP / TB;
     constexpr int kMaxBatch = 4; // slots whose loads are issued together
     const int c = blockIdx.x, G = gridDim.x;
     float *const X = pr.X;
@@ -363,24 +377,24 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
     const float eps = pr.eps;
     const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
     const int a0 = (tid % L::AG) * L::APT, r0 = (tid / L::AG) * L::RPT;
-    const int ga0 = (tid >> 4) * GB, gb0 = (tid & 15) * GB;
+    const int ga0 = (tid / TB) * GB, gb0 = (tid % TB) * GB2;
     float *const gpc = pr.gp + (size_t)c * E;
     const float *sD = sG;
-    auto bar = [] { __syncthreads(); };
-    float gacc[GB][GB];
+    auto bar = [] { tail_sync<NT, SUBSET>(); };
+    float gacc[GB][GB2];
 #pragma unroll
     for (int i = 0; i < GB; i++)
 #pragma unroll
-        for (int k = 0; k < GB; k++) gacc[i][k] = 0.f;
+        for (int k = 0; k < GB2; k++) gacc[i][k] = 0.f;
 #pragma unroll 1
     for (long long xb = x0; xb < x1; xb += 64) {
         const int nr = (int)min(64LL, x1 - xb);
         if (xb != x0) {  // later chunks (more than 64 rows per CTA): stage, reload G, denominators
-            __syncthreads();
+            tail_sync<NT, SUBSET>();
             stage_rows<NP, NT>(X, is_w, rows, r, xb, nr, sX, tid);
             for (int k = tid; k < E / 4; k += NT)
                 reinterpret_cast<float4 *>(sG)[k] = __ldcg(reinterpret_cast<const float4 *>(pr.G_full) + k);
-            __syncthreads();
+            tail_sync<NT, SUBSET>();
             chunk_denominators<NP, NT>(sX, sG, tid, bar);
         }
         const int t0 = (int)(xb / kTileM), t1 = (int)((xb + nr - 1) / kTileM);  // t1 <= t0 + 1
@@ -408,7 +422,7 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             sSl[u * (kFusedSlots + 1)] = ns;
             for (int q = 0; q < ns; q++) sSl[u * (kFusedSlots + 1) + 1 + q] = pr.slot_list[q0 + q];
         }
-        __syncthreads();      // thread 0's acquire loads and this barrier order the slot reads below
+        tail_sync<NT, SUBSET>();      // thread 0's acquire loads and this barrier order the slot reads below
         if (!*sflag) return;  // uniform
         float num[L::RPT][L::APT];
 #pragma unroll
@@ -469,14 +483,14 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
                 }
                 num[k][q] = v;
             }
-        __syncthreads();  // old rows and partial slots read by every thread
+        tail_sync<NT, SUBSET>();  // old rows and partial slots read by every thread
 #pragma unroll
         for (int k = 0; k < L::RPT; k++)
 #pragma unroll
             for (int cc = 0; cc < L::APT / 4; cc++)
                 *reinterpret_cast<float4 *>(sX + (r0 + k) * L::LDX + a0 + 4 * cc) =
                     make_float4(num[k][4 * cc], num[k][4 * cc + 1], num[k][4 * cc + 2], num[k][4 * cc + 3]);
-        __syncthreads();
+        tail_sync<NT, SUBSET>();
 #pragma unroll 4
         for (int kk = 0; kk < L::SL; kk++) {
             const int k = tid + kk * NT;
@@ -497,13 +511,13 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
         // this chunk's new rows into this CTA's Gram partial, rows in order
 #pragma unroll 4
         for (int rr = 0; rr < nr; rr++) {
-            float xa[GB], xb2[GB];
+            float xa[GB], xb2[GB2];
             lds_vec<GB>(sX + rr * L::LDX + ga0, xa);
-            lds_vec<GB>(sX + rr * L::LDX + gb0, xb2);
+            lds_vec<GB2>(sX + rr * L::LDX + gb0, xb2);
 #pragma unroll
             for (int i = 0; i < GB; i++)
 #pragma unroll
-                for (int k = 0; k < GB; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
+                for (int k = 0; k < GB2; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
         }
         if (tid == 0) {
             if (rd0 == last0) {
@@ -522,13 +536,13 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
 #pragma unroll
         for (int i = 0; i < GB; i++) {
             float *dst = gpc + (ga0 + i) * NP + gb0;
-            if constexpr (GB == 4) {
+            if constexpr (GB2 == 4) {
                 *reinterpret_cast<float4 *>(dst) = make_float4(gacc[i][0], gacc[i][1], gacc[i][2], gacc[i][3]);
-            } else if constexpr (GB == 2) {
+            } else if constexpr (GB2 == 2) {
                 *reinterpret_cast<float2 *>(dst) = make_float2(gacc[i][0], gacc[i][1]);
             } else {
 #pragma unroll
-                for (int k = 0; k < GB; k++) dst[k] = gacc[i][k];
+                for (int k = 0; k < GB2; k++) dst[k] = gacc[i][k];
             }
         }
     }
@@ -561,30 +575,58 @@ __global__ void __launch_bounds__(64) gram_partials_kernel(const float *__restri
     for (int k = 0; k < L::NPT; k++) out[(size_t)c * NP * NP + ga * NP + gb0 + k] = gacc[k];
 }
 
-// threads of the GEMM: producer, MMA issuer, four TMEM-draining warps, and with a fused update
-// two worker warps
-__host__ __device__ constexpr int gemm_threads(int fnp) { return fnp ? kGemmThreads + 64 : kGemmThreads; }
+// threads of the GEMM: producer, MMA issuer, four TMEM-draining warps, with a fused update two
+// worker warps, and with a folded quality sample eight quality warps (warps 8-15)
+__host__ __device__ constexpr int gemm_threads(int fnp, bool qf = false) {
+    return (fnp ? kGemmThreads + 64 : kGemmThreads) + (qf ? 256 : 0);
+}
+constexpr int kQfWarps = 8;
+constexpr uint32_t kQfTmemS = 128;  // TMEM column of the first of the two 128-column S buffers
 
-template <int FNP>
-__global__ void __launch_bounds__(gemm_threads(FNP), 1)
+// The hardware's approximate base-2 logarithm (lg2.approx.ftz.f32): its argument s + eps is at
+// least eps >= 1e-30 (s >= 0), a normal float, so flushing subnormals changes nothing.
+__device__ __forceinline__ float lg2_approx(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// QF: the H-step also samples the quality of the factors it starts from (the value
+// NMF::DetermineQualityImprovement reads, nmf_base.h:70-89), on the V tiles it streams anyway:
+// per block (128 columns u of V x 128 rows i) one more MMA forms S = H' W over the block
+// (A: the tile's columns of H, from Hb, MN-major, loaded once per segment; B: the stage's W tile,
+// read MN-major -- the same bytes the main product reads K-major), into one of two 128-column TMEM
+// buffers, and eight quality warps (two per TMEM lane quarter, 64 columns each) add
+// v log2(s + eps) and s over S and the stage's V tile before the stage is released (copying the V
+// tile into TMEM instead, so the stage could go as soon as its MMAs were done, measured slower:
+// 93.3 vs 89.5 us per iteration with the sample).  The per-CTA sums are combined by the last CTA in
+// CTA order, so the value is deterministic.
+template <int FNP, bool QF = false>
+__global__ void __launch_bounds__(gemm_threads(FNP, QF), 1)
     tc_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                      SkParams p) {
+                      const __grid_constant__ CUtensorMap tmQ, SkParams p) {
     const uintptr_t base = (reinterpret_cast<uintptr_t>(tc_dyn_smem) + 1023) & ~uintptr_t(1023);
     const int boxB = p.npad * kBlockK * 2;          // one 64-wide B box
     const int stageA = kStageABytes * p.bps, stageB = boxB * p.bps;
+    const int qslot = QF ? 2 * boxB : 0;            // two 64-column boxes of H's tile columns
     unsigned char *sA = reinterpret_cast<unsigned char *>(base);
     unsigned char *sB = sA + p.stages * stageA;
-    uint64_t *full = reinterpret_cast<uint64_t *>(sB + p.stages * stageB);
+    unsigned char *sQ = sB + p.stages * stageB;     // [2][qslot] (QF)
+    uint64_t *full = reinterpret_cast<uint64_t *>(sQ + 2 * qslot);
     uint64_t *empty = full + p.stages;
     uint64_t *tfull = empty + p.stages;  // [2]
     uint64_t *tempty = tfull + 2;        // [2]
     uint64_t *mdone = tempty + 2;        // [1]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+    uint64_t *qfull = mdone + 1;         // QF: [2] H tile loaded, [2] free, [2] S ready, [2] S drained
+    uint64_t *qempty = qfull + 2, *sfull = qempty + 2, *sempty = sfull + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(QF ? sempty + 2 : mdone + 1);
     // fused-update areas (FNP > 0): Gram, 64-row staging tile, flag
     float *sG = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tmem_slot + 4) + 15) & ~uintptr_t(15));
     float *sX = sG + fused_gram_floats(FNP);
     int *sflag = reinterpret_cast<int *>(sX + 64 * (FNP + 4));
     int *sSl = sflag + 4;
+    double *qred = reinterpret_cast<double *>(sSl + 2 * (kFusedSlots + 1));  // QF: [2][kQfWarps]
+    const uint32_t tcols = QF ? 512u : p.tmem_cols;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long T = (long long)p.tiles * p.kblocks;
@@ -594,22 +636,29 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], QF ? 1 + kQfWarps : 1);  // the MMAs, and the quality warps' V reads
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(&tfull[a], 1);
             mbar_init(&tempty[a], 4);
+            if constexpr (QF) {
+                mbar_init(&qfull[a], 1);
+                mbar_init(&qempty[a], 1);
+                mbar_init(&sfull[a], 1);
+                mbar_init(&sempty[a], kQfWarps);
+            }
         }
         mbar_init(mdone, 1);
         fence_mbar_init();
     }
     if (warp == 0) {
-        tmem_alloc(tmem_slot, p.tmem_cols);
+        tmem_alloc(tmem_slot, tcols);
         tmem_relinquish();
     }
     if (threadIdx.x == 0) {
         tma_prefetch_desc(&tmA);
         tma_prefetch_desc(&tmB);
+        if constexpr (QF) tma_prefetch_desc(&tmQ);
     }
     tc_fence_before();
     __syncthreads();
@@ -626,6 +675,31 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             uint32_t phase = 0;
             int armed[kMaxStages];
             for (int s = 0; s < kMaxStages; s++) armed[s] = 0;
+            // QF: the H tile of each segment (the columns u of its row tile), into slot qs
+            int qcur = -1, qs = 0, qloads = 0, qarmed[2] = {0, 0};
+            uint32_t qph = 0;
+            bool qok = true;
+            auto load_q = [&](int t) {
+                if constexpr (QF) {
+                    if (t == qcur || !qok) return;
+                    if (qloads >= 2 && !mbar_wait(&qempty[qs], qph ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) {
+                        qok = false;
+                        return;
+                    }
+                    mbar_arrive_expect_tx(&qfull[qs], (uint32_t)qslot);
+                    for (int q = 0; q < 2; q++)
+                        tma_load_2d(sQ + qs * qslot + q * boxB, &tmQ, t * kTileM + q * 64, 0, &qfull[qs]);
+                    qarmed[qs]++;
+                    qloads++;
+                    qcur = t;
+                    if (++qs == 2) {
+                        qs = 0;
+                        qph ^= 1;
+                    }
+                } else {
+                    (void)t;
+                }
+            };
             const int pre = (int)min((long long)p.stages, hi - lo);  // fresh stages: no empty wait
             for (int i = 0; i < pre; i++) {
                 const long long b = lo + i;
@@ -639,6 +713,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             griddep_launch_dependents();
             for (int i = 0; i < pre; i++) {
                 const int kb = (int)((lo + i) % p.kblocks);
+                load_q((int)((lo + i) / p.kblocks));
                 for (int q = 0; q < p.bps; q++)
                     tma_load_2d(sB + i * stageB + q * boxB, &tmB, (kb * p.bps + q) * kBlockK, 0, &full[i]);
                 armed[i]++;
@@ -647,7 +722,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             phase = pre == p.stages ? 1u : 0u;
             for (long long b = lo + pre; b < hi; b++) {
                 const int t = (int)(b / p.kblocks), kb = (int)(b % p.kblocks);
-                if (!mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) break;
+                load_q(t);
+                if (!qok || !mbar_wait(&empty[stage], phase ^ 1, p.err, kErrWaitEmpty, p.wait_limit)) break;
                 mbar_arrive_expect_tx(&full[stage], stageA + stageB);
                 // adjacent boxes along K: each row's bytes of the stage are requested back to back
                 for (int q = 0; q < p.bps; q++)
@@ -665,6 +741,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 // error exit: let the copies already issued land before the CTA leaves
                 for (int s = 0; s < p.stages; s++)
                     if (armed[s] > 0) mbar_wait_quiet(&full[s], (uint32_t)((armed[s] - 1) & 1));
+                for (int s = 0; s < 2; s++)
+                    if (qarmed[s] > 0) mbar_wait_quiet(&qfull[s], (uint32_t)((qarmed[s] - 1) & 1));
             }
         } else {
             griddep_wait();
@@ -675,13 +753,18 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
         griddep_launch_dependents();
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16_f32(kTileM, p.npad);
-            int stage = 0, acc = 0;
-            uint32_t phase = 0, aphase = 0;
+            // S = H' W over a block: both operands MN-major, the second 64 of M / N one box further
+            const uint32_t idesc_q = idesc_bf16_f32(kTileM, 128) | kIdescAMnMajor | kIdescBMnMajor;
+            int stage = 0, acc = 0, qs = 0, sb = 0;
+            uint32_t phase = 0, aphase = 0, qph = 0, sph = 0;
             bool ok = true;
             for (long long b = lo; b < hi && ok;) {
                 const long long t = b / p.kblocks;
                 const long long e = min(hi, (t + 1) * p.kblocks);
                 if (!mbar_wait(&tempty[acc], aphase ^ 1, p.err, kErrWaitTmemEmpty, p.wait_limit)) break;
+                if constexpr (QF) {
+                    if (!mbar_wait(&qfull[qs], qph, p.err, kErrWaitFull, p.wait_limit)) break;
+                }
                 tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(acc * p.npad);
                 for (long long bb = b; bb < e; bb++) {
@@ -699,6 +782,22 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                                        idesc, (bb > b || q > 0 || k > 0) ? 1u : 0u);
                         }
                     }
+                    if constexpr (QF) {
+                        if (!mbar_wait(&sempty[sb], sph ^ 1, p.err, kErrWaitTmemEmpty, p.wait_limit)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t qa = smem_u32(sQ + qs * qslot), qb = smem_u32(sB + stage * stageB);
+                        for (int k16 = 0; k16 < p.npad / 16; k16++)
+                            tc_mma_f16(tmem + kQfTmemS + (uint32_t)(sb * 128), smem_desc(qa + k16 * 2048, boxB, 1024, 2),
+                                       smem_desc(qb + k16 * 2048, boxB, 1024, 2), idesc_q, k16 > 0 ? 1u : 0u);
+                        tc_commit(&sfull[sb]);
+                        if (++sb == 2) {
+                            sb = 0;
+                            sph ^= 1;
+                        }
+                    }
                     tc_commit(&empty[stage]);
                     if (++stage == p.stages) {
                         stage = 0;
@@ -710,6 +809,13 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
                 if (++acc == 2) {
                     acc = 0;
                     aphase ^= 1;
+                }
+                if constexpr (QF) {
+                    tc_commit(&qempty[qs]);  // the segment's H tile is free once its MMAs complete
+                    if (++qs == 2) {
+                        qs = 0;
+                        qph ^= 1;
+                    }
                 }
                 b = e;
             }
@@ -789,20 +895,132 @@ __global__ void __launch_bounds__(gemm_threads(FNP), 1)
             b = e;
         }
     } else if constexpr (FNP > 0) {
+      if (warp < 8) {
         griddep_wait();
         griddep_launch_dependents();
         fused_prologue<FNP>(p, threadIdx.x - kGemmThreads, sG, sX, sflag);  // warps 6 and 7
+      } else if constexpr (QF) {
+        griddep_wait();
+        griddep_launch_dependents();
+        // quality warps 8-15: warp w reads TMEM lane quarter w % 4 (the block's rows u), columns
+        // 64 * half .. of S (rows i of the block, the stage's V box `half`)
+        const int qw = warp - 8, quarter = warp & 3, half = qw >> 2;
+        const int row = quarter * 32 + lane;
+        const float eps = fmaxf(p.qeps, 1e-30f);
+        double dlog = 0.0, ds = 0.0;
+        int stage = 0, sb = 0;
+        uint32_t phase = 0, sph = 0;
+        for (long long b = lo; b < hi; b++) {
+            if (!warp_wait(&sfull[sb], sph, p.err, kErrWaitTmemFull, p.wait_limit)) break;
+            if (!warp_wait(&full[stage], phase, p.err, kErrWaitFull, p.wait_limit)) break;  // the V tile
+            tc_fence_after();
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + kQfTmemS + (uint32_t)(sb * 128 + half * 64);
+            const unsigned char *vrow = sA + stage * stageA + half * kStageABytes + row * 128;
+            // four independent sums each (the chain of one would be the epilogue's critical path)
+            float plog[4] = {0.f, 0.f, 0.f, 0.f}, ps[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int c2 = 0; c2 < 2; c2++) {  // 32 columns at a time
+                float sv[32];
+                {
+                    float (&s0)[16] = *reinterpret_cast<float (*)[16]>(&sv[0]);
+                    float (&s1)[16] = *reinterpret_cast<float (*)[16]>(&sv[16]);
+                    tmem_ld16(taddr + (uint32_t)(c2 * 32), s0);
+                    tmem_ld16(taddr + (uint32_t)(c2 * 32 + 16), s1);
+                }
+                uint4 raw[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    raw[k] = *reinterpret_cast<const uint4 *>(vrow + (((c2 * 4 + k) ^ (row & 7)) << 4));
+                tmem_ld_wait();
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&raw[k]);
+#pragma unroll
+                    for (int e2 = 0; e2 < 4; e2++) {
+                        const float2 vv = __bfloat1622float2(h2[e2]);
+                        const int j = 8 * k + 2 * e2;
+                        plog[e2] = fmaf(vv.x, lg2_approx(sv[j] + eps), plog[e2]);
+                        plog[e2] = fmaf(vv.y, lg2_approx(sv[j + 1] + eps), plog[e2]);
+                        ps[e2] += sv[j];
+                        ps[e2] += sv[j + 1];
+                    }
+                }
+            }
+            dlog += (double)((plog[0] + plog[1]) + (plog[2] + plog[3]));
+            ds += (double)((ps[0] + ps[1]) + (ps[2] + ps[3]));
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&sempty[sb]);
+                mbar_arrive(&empty[stage]);
+            }
+            if (++stage == p.stages) {
+                stage = 0;
+                phase ^= 1;
+            }
+            if (++sb == 2) {
+                sb = 0;
+                sph ^= 1;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            dlog += __shfl_down_sync(0xffffffffu, dlog, off);
+            ds += __shfl_down_sync(0xffffffffu, ds, off);
+        }
+        if (lane == 0) {
+            qred[qw] = dlog;
+            qred[kQfWarps + qw] = ds;
+        }
+        asm volatile("bar.sync 5, 256;" ::: "memory");  // the eight quality warps
+        if (qw == 0) {
+            if (lane == 0) {
+                double l = 0.0, sm = 0.0;
+                for (int w = 0; w < kQfWarps; w++) {
+                    l += qred[w];
+                    sm += qred[kQfWarps + w];
+                }
+                p.qpartial[blockIdx.x] = 0.30102999566398120 * l - sm;  // log10(x) = log2(x) log10(2)
+                // publishes this partial; the last CTA's add also acquires every other CTA's
+                reinterpret_cast<volatile int *>(qred)[0] = atom_acq_rel_add(p.qdone, 1) == (int)gridDim.x - 1;
+            }
+            __syncwarp();
+            if (reinterpret_cast<volatile int *>(qred)[0]) {
+                // the last CTA: the partials summed in CTA order (lane-strided, then a fixed tree)
+                double q = 0.0;
+                for (int c = lane; c < (int)gridDim.x; c += 32) q += __ldcg(p.qpartial + c);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) q += __shfl_down_sync(0xffffffffu, q, off);
+                if (lane == 0) {
+                    p.qout[0] = (float)q;
+                    if (p.qout_host) {
+                        p.qout_host[0] = (float)q;
+                        __threadfence_system();
+                    }
+                    *p.qdone = 0;
+                }
+            }
+        }
+    }
     }
     __syncthreads();
     if constexpr (FNP > 0) {
-        // every role is done: all threads finish the update (skipped, uniformly, after an error)
+        // every role is done: the threads finish the update (skipped, uniformly, after an error) --
+        // with quality warps at rank 64 all 512 (half the rows per thread: nothing spills at the
+        // 128 registers a 512-thread CTA allows), at rank 32 the first 256
         const bool go = __syncthreads_and(*((volatile int *)p.err) == 0);
-        if (go) fused_tail<FNP>(p, threadIdx.x, sG, sX, sflag, sSl);
+        if constexpr (QF && FNP == 64) {
+            if (go) fused_tail<FNP, 512, false>(p, threadIdx.x, sG, sX, sflag, sSl);
+        } else if constexpr (QF) {
+            if (go && threadIdx.x < 256) fused_tail<FNP, 256, true>(p, threadIdx.x, sG, sX, sflag, sSl);
+        } else {
+            if (go) fused_tail<FNP, 256, false>(p, threadIdx.x, sG, sX, sflag, sSl);
+        }
         __syncthreads();
     }
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tmem, p.tmem_cols);
+        tmem_dealloc(tmem, tcols);
     }
 }
 
@@ -823,13 +1041,6 @@ constexpr int kQThreads = 64 + 32 * kQEpiWarps;
 constexpr int kQTile = 128;
 constexpr int kQVBytes = kQTile * kQTile * 2;
 
-// The hardware's approximate base-2 logarithm (lg2.approx.ftz.f32): its argument s + eps is at
-// least eps >= 1e-30 (s >= 0), a normal float, so flushing subnormals changes nothing.
-__device__ __forceinline__ float lg2_approx(float x) {
-    float y;
-    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
 
 struct QParams {
     int tiles_i, tiles_u, npad, stages;
@@ -1004,7 +1215,7 @@ __global__ void __launch_bounds__(kQThreads, 1)
             // this row's 32 values of V: 4 chunks of 8 in the 128-byte swizzled row i of box c0 / 64
             const unsigned char *vrow =
                 reinterpret_cast<const unsigned char *>(v + (c0 >> 6) * (kQTile * 64)) + i * 128;
-            float plog = 0.f, ps = 0.f;
+            float plog[4] = {0.f, 0.f, 0.f, 0.f}, ps[4] = {0.f, 0.f, 0.f, 0.f};  // four independent sums each
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 const int chunk = (((c0 & 63) >> 3) + k) ^ (i & 7);
@@ -1014,14 +1225,14 @@ __global__ void __launch_bounds__(kQThreads, 1)
                 for (int e = 0; e < 4; e++) {
                     const float2 vv = __bfloat1622float2(h2[e]);
                     const int j = 8 * k + 2 * e;
-                    plog = fmaf(vv.x, lg2_approx(sv[j] + eps), plog);
-                    plog = fmaf(vv.y, lg2_approx(sv[j + 1] + eps), plog);
-                    ps += sv[j];
-                    ps += sv[j + 1];
+                    plog[e] = fmaf(vv.x, lg2_approx(sv[j] + eps), plog[e]);
+                    plog[e] = fmaf(vv.y, lg2_approx(sv[j + 1] + eps), plog[e]);
+                    ps[e] += sv[j];
+                    ps[e] += sv[j + 1];
                 }
             }
-            dlog += (double)plog;
-            ds += (double)ps;
+            dlog += (double)((plog[0] + plog[1]) + (plog[2] + plog[3]));
+            ds += (double)((ps[0] + ps[1]) + (ps[2] + ps[3]));
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -2128,9 +2339,11 @@ __global__ void convert_rowmajor_kernel(const float *__restrict__ X, int rows, i
 
 struct TcGemm {
     CUtensorMap tmA, tmB;
+    CUtensorMap tmQ;  // H-step with a folded quality sample: Hb, boxes of 64 columns u x npad rows
     gpunmf::SkParams p;
     int grid = 0;
     int smem = 0;
+    int smem_qf = 0;  // shared memory of the variant with the quality warps
     int fnp = 0;  // fused update rank (kernel template argument), 0 = separate update kernel
     int *slot_ptr = nullptr, *slot_list = nullptr;
     int *tile_slots = nullptr;
@@ -2169,6 +2382,8 @@ struct TcState {
     int qgrid = 0, qsmem = 0;
     float *GP_w = nullptr, *GP_h = nullptr;   // per-CTA Gram partials of the update kernels
     int gp_w_count = 0, gp_h_count = 0;
+    bool qfold = false;        // the quality sample can ride on the H-step (fused Euclidean jobs)
+    bool qfold_armed = false;  // the next H-step carries it
     int max_ctas = 0;                         // CTAs per launch: the SMs, or fewer (gpunmf_set_grid_limit)
 };
 
@@ -2329,6 +2544,8 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     g.p.err = err;
     g.p.wait_limit = kWaitLimitCycles;
     g.smem = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16 + (fnp ? 16 + fused_smem_bytes(fnp) : 0);
+    // with the folded quality sample: two H-tile slots, eight more barriers, the warps' sums
+    g.smem_qf = g.smem + 2 * 2 * npad * kBlockK * 2 + 8 * 8 + 2 * kQfWarps * 8;
     g.fnp = fnp;
     size_t slots = (size_t)g.grid * max_seg;
     cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
@@ -2429,6 +2646,10 @@ static cudaError_t set_gemm_smem_once() {
             result = cudaFuncSetAttribute(tc_gemm_sk_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
         if (result == cudaSuccess)
             result = cudaFuncSetAttribute(tc_gemm_sk_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (result == cudaSuccess)
+            result = cudaFuncSetAttribute(tc_gemm_sk_kernel<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (result == cudaSuccess)
+            result = cudaFuncSetAttribute(tc_gemm_sk_kernel<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
     return result;
 }
@@ -2875,7 +3096,25 @@ static gpunmf_status setup_quality(gpunmf_job *j) {
         return GPUNMF_ERR_CUDA;
     }
     q.partial = j->red;
+    // fused Euclidean jobs with an H-step sample the quality inside it (the H-step streams the same V)
+    TcGemm &g = t->gh;
+    if (g.fnp && j->rule != GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H && g.p.bps == 2 && (size_t)g.grid <= j->red_cap &&
+        g.smem_qf <= smem_optin()) {
+        g.tmQ = t->tmQB;
+        g.p.qeps = j->eps;
+        g.p.qpartial = j->red;
+        g.p.qdone = q.done;
+        g.p.qout = j->d_quality;
+        g.p.qout_host = q.out_host;
+        t->qfold = true;
+    }
     return GPUNMF_OK;
+}
+
+bool tc_quality_fold(gpunmf_job *j) {
+    if (!j->tc || !j->tc->qfold) return false;
+    j->tc->qfold_armed = true;
+    return true;
 }
 
 bool tc_quality_ready(const gpunmf_job *j) { return j->tc && j->tc->qp.partial != nullptr; }
@@ -3072,27 +3311,32 @@ gpunmf_status tc_prepare(gpunmf_job *j, const float *v_src) {
     return GPUNMF_OK;
 }
 
-static cudaError_t launch_gemm_cfg(TcGemm &g, cudaLaunchConfig_t &cfg) {
+static cudaError_t launch_gemm_cfg(TcGemm &g, cudaLaunchConfig_t &cfg, bool qf) {
+    // (kernels without quality warps never read the third map)
+    if (qf) {
+        if (g.fnp == 32) return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<32, true>, g.tmA, g.tmB, g.tmQ, g.p);
+        return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<64, true>, g.tmA, g.tmB, g.tmQ, g.p);
+    }
     switch (g.fnp) {
-        case 32: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<32>, g.tmA, g.tmB, g.p);
-        case 64: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<64>, g.tmA, g.tmB, g.p);
-        default: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<0>, g.tmA, g.tmB, g.p);
+        case 32: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<32>, g.tmA, g.tmB, g.tmB, g.p);
+        case 64: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<64>, g.tmA, g.tmB, g.tmB, g.p);
+        default: return cudaLaunchKernelEx(&cfg, tc_gemm_sk_kernel<0>, g.tmA, g.tmB, g.tmB, g.p);
     }
 }
 
-static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s) {
+static cudaError_t launch_gemm(TcGemm &g, cudaStream_t s, bool qf = false) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.grid);
-    cfg.blockDim = dim3(gemm_threads(g.fnp));
-    cfg.dynamicSmemBytes = g.smem;
+    cfg.blockDim = dim3(gemm_threads(g.fnp, qf));
+    cfg.dynamicSmemBytes = qf ? g.smem_qf : g.smem;
     cfg.stream = s;
     cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if (!g.fnp) return launch_gemm_cfg(g, cfg);
-    return launch_resident(cfg, at, [&] { return launch_gemm_cfg(g, cfg); });
+    if (!g.fnp) return launch_gemm_cfg(g, cfg, false);
+    return launch_resident(cfg, at, [&] { return launch_gemm_cfg(g, cfg, qf); });
 }
 
 gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
@@ -3124,10 +3368,18 @@ gpunmf_status tc_iterate(gpunmf_job *j, bool updateW) {
     if (t->gh.fnp) {
         // one launch per half-step: the GEMM's last arrivals update the factor and its Gram
         if (j->rule != GPUNMF_ADDITIVE_EUCLIDEAN_FIXED_H) {
+            const bool qf = t->qfold_armed;  // this H-step also samples the quality
+            t->qfold_armed = false;
             mark_begin(j);
-            GPUNMF_CUDA_TRY(launch_gemm(t->gh, s));
+            GPUNMF_CUDA_TRY(launch_gemm(t->gh, s, qf));
             mark_end(j);
             j->launches += 1;
+            if (qf) {
+                if (!tc_quality_writes_host(j))
+                    GPUNMF_CUDA_TRY(cudaMemcpyAsync(j->h_quality(), j->d_quality, sizeof(float), cudaMemcpyDeviceToHost, s));
+                GPUNMF_CUDA_TRY(cudaEventRecord(j->qev, s));
+                j->q_pending = true;
+            }
         }
         if (!updateW) return GPUNMF_OK;
         mark_begin(j);
