@@ -49,12 +49,12 @@ METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from the committed ncu
 # captures of this workload (one --set full capture per precision, see the profiles
-# directory): tc_gemm_sk_kernel<64> with the update fused in 139.73 MB + 3.60 MB;
-# gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
-NCU_TRAFFIC_PER_LAUNCH = {"bf16": 143.34e6, "fp32": 276.09e6}
+# directory): tc_gemm_sk_kernel<64> with the update fused, mean of an H-step and a W-step launch,
+# 139.36 MB + 3.35 MB; gemm_f32_kernel (W'V) 272.95 MB + 3.14 MB.
+NCU_TRAFFIC_PER_LAUNCH = {"bf16": 142.71e6, "fp32": 276.09e6}
 # The same for the KL workload's fused product (tc_kl_gemm_kernel<8> with the update fused, mean of
-# an H-step and a W-step launch: 140.40 MB + 4.33 MB).
-KL_NCU_TRAFFIC_PER_LAUNCH = {"bf16": 144.73e6}
+# an H-step and a W-step launch: 139.87 MB + 3.90 MB).
+KL_NCU_TRAFFIC_PER_LAUNCH = {"bf16": 143.77e6}
 
 
 def parse():

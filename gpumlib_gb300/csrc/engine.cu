@@ -289,29 +289,23 @@ static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int pre
     return GPUNMF_OK;
 }
 
-// The address at which kernels of the current device read host matrix p, or null: page-locked memory
-// mapped into the device's address space, or any host memory where the device reads pageable memory
-// through the host's page tables (coherent CPU-GPU systems).
+// The address at which kernels of the current device read host matrix p, or null: page-locked
+// memory mapped into the device's address space.  (Pageable memory is readable too where the device
+// uses the host page tables, but the conversion kernel's reads of it ran at ~116 GB/s against
+// ~210 GB/s for a copy, so pageable matrices are copied first.)
 static const float *device_readable_host(const float *p) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
         return static_cast<const float *>(a.devicePointer);
-    cudaGetLastError();
-    int dev = 0, pageable = 0, host_tables = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess &&
-        pageable && host_tables && (a.type == cudaMemoryTypeUnregistered))
-        return p;
     cudaGetLastError();
     return nullptr;
 }
 
 static gpunmf_status job_upload(gpunmf_job *j, const float *V, const float *W, const float *H, cudaMemcpyKind kind) {
     size_t nm = (size_t)j->n * j->m, nr = (size_t)j->n * j->r, rm = (size_t)j->r * j->m;
-    // BF16 jobs from host memory the device can read: V crosses the host link once, read by the
-    // conversion kernel that writes its BF16 copies and the FP32 copy (a copy first and a conversion
-    // after would move V twice through device memory)
+    // BF16 jobs from page-locked host memory: V crosses the host link once, read by the conversion
+    // kernel that writes its BF16 copies and the FP32 copy (a copy first and a conversion after
+    // would move V through device memory twice more)
     const float *v_src = (kind == cudaMemcpyHostToDevice && j->precision == GPUNMF_BF16) ? device_readable_host(V)
                                                                                         : nullptr;
     if (!v_src) GPUNMF_CUDA_TRY(cudaMemcpyAsync(j->V, V, nm * sizeof(float), kind, j->stream));
