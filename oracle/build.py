@@ -12,16 +12,33 @@
   written for MSVC and fails g++'s two-phase lookup) and whose include of
   HostMatrix.h is made absolute.  Everything lands in the git-ignored
   oracle/_ref/.
+* ``build_ref_faces()`` compiles the reference's own FacesNMF image loader:
+  the definitions of ``CFacesNMFDlg::FolderHasImages`` and
+  ``CFacesNMFDlg::LoadImage`` are copied unchanged out of
+  src/examples/FacesNMF/FacesNMFDlg.cpp into oracle/_ref/faces_dlg_methods.inc
+  and built with oracle/ref_faces_shim.cpp (plain C++ stand-ins for the MFC
+  names they use) into oracle/_ref/libfaces_ref.so.
+* ``stage_faces_images()`` copies the data set (src/examples/FacesNMF/images,
+  2429 P5 files of 19 x 19) into oracle/_ref/faces_images/, where the GPU
+  tests find it on a machine without the reference tree.
+
+The reference root is one setting: the environment variable
+GPUNMF_REFERENCE_ROOT, else DEFAULT_REFERENCE_ROOT below.  Without a reference
+tree there, every builder here returns None and the tests that need the
+reference's own code skip; the committed golden vectors carry the checks.
 """
 import os
 import re
+import shutil
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(HERE, "_lib")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("GPUNMF_REFERENCE_ROOT", "/root/reference")
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("GPUNMF_REFERENCE_ROOT", DEFAULT_REFERENCE_ROOT)
+FACES_IMAGES = os.path.join(REF_DIR, "faces_images")
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
@@ -91,6 +108,81 @@ def build_ref(force=False):
     return out
 
 
+def _definition(text, signature):
+    """The text of the function definition that starts with `signature`, through its closing brace."""
+    start = text.index(signature)
+    open_at = text.index("{", start)
+    depth = 0
+    for i in range(open_at, len(text)):
+        if text[i] == "{":
+            depth += 1
+        elif text[i] == "}":
+            depth -= 1
+            if depth == 0:
+                return text[start:i + 1]
+    raise ValueError("unbalanced braces after " + signature)
+
+
+def build_ref_faces(force=False):
+    """Build oracle/_ref/libfaces_ref.so from the reference's loader; returns its path or None."""
+    if not reference_available():
+        return None
+    build_ref(force)   # writes the generated Matrix.h the loader's Matrix<cudafloat> needs
+    faces = os.path.join(REFERENCE_ROOT, "src/examples/FacesNMF")
+    shim = os.path.join(HERE, "ref_faces_shim.cpp")
+    out = os.path.join(REF_DIR, "libfaces_ref.so")
+    if not force and _newer(out, [shim, __file__]):
+        return out
+    with open(os.path.join(faces, "FacesNMFDlg.cpp"), "r", encoding="latin-1") as f:
+        text = f.read()
+    methods = [_definition(text, "bool CFacesNMFDlg::FolderHasImages("),
+               _definition(text, "bool CFacesNMFDlg::LoadImage(")]
+    with open(os.path.join(REF_DIR, "faces_dlg_methods.inc"), "w", encoding="latin-1") as f:
+        f.write("// copied unchanged from src/examples/FacesNMF/FacesNMFDlg.cpp by oracle/build.py\n")
+        f.write("\n\n".join(methods) + "\n")
+    cmd = ["g++", "-std=c++14", *CFLAGS, "-w",
+           "-I", REF_DIR,
+           "-I", os.path.join(REFERENCE_ROOT, "src/cuda"),
+           "-I", os.path.join(REFERENCE_ROOT, "src/memory"),
+           "-I", os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/include",
+           shim, "-o", out,
+           "-L", os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/lib64", "-lcudart"]
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def stage_faces_images():
+    """Copy the FacesNMF data set into oracle/_ref/faces_images/; returns the folder or None."""
+    src = os.path.join(REFERENCE_ROOT, "src/examples/FacesNMF/images")
+    if not os.path.isdir(src):
+        return FACES_IMAGES if os.path.isdir(FACES_IMAGES) else None
+    os.makedirs(FACES_IMAGES, exist_ok=True)
+    for name in sorted(os.listdir(src)):
+        if not name.endswith(".pgm"):
+            continue
+        dst = os.path.join(FACES_IMAGES, name)
+        if not os.path.exists(dst):
+            shutil.copyfile(os.path.join(src, name), dst)
+    return FACES_IMAGES
+
+
+def backslash_folder(folder, workdir):
+    """A folder name F such that F + "\\" + "faceNNNNN.pgm" names each image of `folder`.
+
+    The reference loader joins folder and file with a backslash
+    (FacesNMFDlg.cpp:315,334,417); on Linux that is part of one file name, so
+    `workdir` receives links named 'x\\faceNNNNN.pgm' to the images."""
+    os.makedirs(workdir, exist_ok=True)
+    for name in os.listdir(folder):
+        if name.startswith("face") and name.endswith(".pgm"):
+            link = os.path.join(workdir, "x\\" + name)
+            if not os.path.lexists(link):
+                os.symlink(os.path.abspath(os.path.join(folder, name)), link)
+    return os.path.join(workdir, "x")
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_faces(force="--force" in sys.argv))
+    print(stage_faces_images())

@@ -9,9 +9,12 @@ whitespace byte that ends the header) unless reference_offset is False, and
 the histogram equalisation is the reference's float arithmetic:
 cumulative counts, cdfmin = the first nonzero one, (cum - cdfmin) /
 (pixels - cdfmin).  scan follows FolderHasImages (:309-347) and csv_text
-follows Save (:913-924) with PRECISION 20 (Definitions.h:31).  The parity of
-this restatement is unpinned: the reference code is an MFC dialog that does
-not build here.
+follows Save (:913-924) with PRECISION 20 (Definitions.h:31).  Pinned bit for
+bit against the reference's own FolderHasImages / LoadImage, compiled from
+FacesNMFDlg.cpp with stand-ins for the MFC names (oracle/ref_faces_shim.cpp),
+on the whole FacesNMF data set and on edge-case images
+(tests/test_faces_real_data.py).  Save is not pinned that way: it writes
+through MFC file dialogs.
 """
 import os
 
