@@ -744,6 +744,24 @@ def run_serving(args, rank, world, local, dist):
             "note": "one_job_at_a_time_fp32 replays the first 5% of the trace through a single slot"}
 
 
+def reference_gpu_classes(V, W, H, iters, warmup):
+    """The reference's own GPU class NMF_MultiplicativeEuclidianDistance (built from its sources for
+    sm_103a with cuBLAS) on the same workload: DoIteration() calls per second, its quality sampling
+    included, as the class runs it.  Its epsilon is fixed at 1e-8 (nmf_kernels.h:34)."""
+    os.environ["NVIDIA_TF32_OVERRIDE"] = "0"   # plain FP32 SGEMM, as the reference's cuBLAS calls ask
+    try:
+        import oracle
+        if oracle.reference_gpu() is None:
+            return {"unavailable": "no reference sources (tree or staged copy) to build its GPU classes from"}
+        _, _, sec = oracle.reference_gpu_run(0, V, W, H, iters, warmup=warmup)
+    except Exception as exc:   # reported, not fatal: the CPU reference is the arm's value
+        return {"unavailable": "%s: %s" % (type(exc).__name__, exc)}
+    return {"value": round(iters / sec, 3), "unit": "iters/s", "iterations": iters, "warmup": warmup,
+            "seconds": round(sec, 4), "precision": "fp32 (cuBLAS SGEMM, TF32 off)", "eps": 1e-8,
+            "what": "reference NMF_MultiplicativeEuclidianDistance::DoIteration() on the GPU, built from its "
+                    "sources for sm_103a; wall time between device synchronisations"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -751,13 +769,15 @@ def run_reference(args, rank, world):
     V, W, H, eps = make_workload(n, m, r)
     # every step (and every warm-up step) is one full-size iteration
     ips, sec, info = cpu_reference_steps(V, W, H, eps, steps=max(1, args.steps), warmup=max(0, args.warmup))
+    gpu_classes = reference_gpu_classes(V, W, H, iters=max(20, args.steps), warmup=max(3, args.warmup))
     return {"impl": "reference", "metric": METRIC, "value": ips, "unit": "iters/s", "n_gpus": world,
             "steps": info["iterations"], "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "precision": "fp32",
             "data": "synthetic (same workload as the engine arm)",
             "config": workload_config(n, m, r, eps, world),
             "cpu_baseline": {"value": ips, "unit": "iters/s", **info},
-            "e2e": {"value": ips, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": ips, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_classes": gpu_classes}
 
 
 def main():

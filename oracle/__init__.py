@@ -1,10 +1,12 @@
 """ctypes access to the CPU oracle (test infrastructure only).
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
-this package, and only as the checker.  ``orc()`` loads the float/double
-restatement built from oracle/nmf_oracle.c; ``ref()`` loads the reference's
-own HostNMF built from its sources (present only where the reference tree
-was available at build time).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg and
+reference arm may use this package, and only as the checker or as the
+reference being timed.  ``orc()`` loads the float/double restatement built
+from oracle/nmf_oracle.c; ``ref()`` loads the reference's own HostNMF built
+from its sources (present only where the reference tree was available at
+build time); ``reference_gpu()`` loads the reference's own GPU classes, built
+for sm_103a from its sources or their staged copy.
 """
 import ctypes
 import os
@@ -62,6 +64,46 @@ def ref():
         lib.ref_hostnmf_time.restype = ctypes.c_double
         _ref = lib
     return _ref
+
+
+_ref_gpu = None
+
+
+def reference_gpu():
+    """The reference's own GPU NMF classes, built from its sources for sm_103a with cuBLAS
+    (oracle/build.py: build_ref_gpu), or None where neither the reference tree nor its staged
+    copy is present.  Needs a GPU to run."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        path = _build.build_ref_gpu()
+        if path is None:
+            return None
+        lib = ctypes.CDLL(path)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        lib.refgpu_init.argtypes = []
+        lib.refgpu_init.restype = i
+        lib.refgpu_run.argtypes = [i, i, i, i, vp, vp, vp, i, i, vp]
+        lib.refgpu_run.restype = i
+        _ref_gpu = lib
+    return _ref_gpu
+
+
+def reference_gpu_run(rule, V, W, H, iters, warmup=0):
+    """(W, H, seconds): the reference's NMF_MultiplicativeEuclidianDistance (rule 0) or
+    NMF_MultiplicativeDivergence (rule 1) constructed from (V, W, H), `warmup` then `iters`
+    DoIteration() calls; seconds is the wall time of the `iters` calls between device
+    synchronisations."""
+    lib = reference_gpu()
+    if lib is None:
+        raise RuntimeError("the reference's GPU classes are not available (no reference sources)")
+    V = _f32_in(V); W = _f32(W); H = _f32(H)
+    n, m = V.shape
+    r = W.shape[1]
+    sec = ctypes.c_double(0.0)
+    rc = lib.refgpu_run(rule, n, m, r, _p(V), _p(W), _p(H), warmup, iters, ctypes.byref(sec))
+    if rc != 0:
+        raise RuntimeError("reference GPU NMF failed with code %d" % rc)
+    return W, H, sec.value
 
 
 def _f32(a):

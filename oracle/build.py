@@ -18,6 +18,13 @@
   src/examples/FacesNMF/FacesNMFDlg.cpp into oracle/_ref/faces_dlg_methods.inc
   and built with oracle/ref_faces_shim.cpp (plain C++ stand-ins for the MFC
   names they use) into oracle/_ref/libfaces_ref.so.
+* ``stage_ref_gpu_sources()`` copies the reference's sources for its GPU NMF
+  classes (the files in REF_GPU_FILES, unchanged, keeping their relative
+  paths) into oracle/_ref/gpu_src/, and ``build_ref_gpu()`` compiles them with
+  oracle/ref_gpu_shim.cu for sm_103a against cuBLAS into
+  oracle/_ref/libref_gpu_nmf.so.  The copies exist because the machine with
+  the GPU has no reference tree: the recipe runs there from the staged copy.
+  They are git-ignored build inputs, never part of the repository.
 * ``stage_faces_images()`` copies the data set (src/examples/FacesNMF/images,
   2429 P5 files of 19 x 19) into oracle/_ref/faces_images/, where the GPU
   tests find it on a machine without the reference tree.
@@ -151,6 +158,58 @@ def build_ref_faces(force=False):
     return out
 
 
+REF_GPU_DIR = os.path.join(REF_DIR, "gpu_src")
+REF_GPU_FILES = [
+    "src/algorithms/nmf/nmf_base.h",
+    "src/algorithms/nmf/nmf_multiplicative_euclidian.h",
+    "src/algorithms/nmf/nmf_multiplicative_euclidian.cpp",
+    "src/algorithms/nmf/nmf_multiplicative_divergence.h",
+    "src/algorithms/nmf/nmf_multiplicative_divergence.cpp",
+    "src/cuda/definitions.h",
+    "src/cuda/nmf/nmf_kernels.h",
+    "src/cuda/nmf/nmf_kernels.cu",
+    "src/cuda/nmf/nmf_kernels_quality.cu",
+    "src/common/CudaStreams.h",
+    "src/common/Utilities.h",
+    "src/common/config.h",
+] + ["src/memory/" + h for h in ("BaseArray.h", "BaseMatrix.h", "DeviceAccessibleVariable.h", "DeviceArray.h",
+                                 "DeviceMatrix.h", "DeviceMemoryManager.h", "HostArray.h", "HostMatrix.h",
+                                 "HostMemoryManager.h", "MemoryManager.h")]
+# the definitions the reference's CMakeLists.txt:119-124 sets for compute capability >= 3.0
+REF_GPU_DEFINES = ["-DCUDA_MAX_THREADS_PER_BLOCK=1024", "-DCUDA_MAX_GRID_X_DIM=2147483647"]
+
+
+def stage_ref_gpu_sources():
+    """Copy REF_GPU_FILES into oracle/_ref/gpu_src/; returns that folder, or None without sources."""
+    if os.path.isdir(os.path.join(REFERENCE_ROOT, "src")):
+        for rel in REF_GPU_FILES:
+            src, dst = os.path.join(REFERENCE_ROOT, rel), os.path.join(REF_GPU_DIR, rel)
+            os.makedirs(os.path.dirname(dst), exist_ok=True)
+            if not (os.path.isfile(dst) and open(src, "rb").read() == open(dst, "rb").read()):
+                shutil.copyfile(src, dst)
+    if all(os.path.isfile(os.path.join(REF_GPU_DIR, rel)) for rel in REF_GPU_FILES):
+        return REF_GPU_DIR
+    return None
+
+
+def build_ref_gpu(force=False):
+    """Build oracle/_ref/libref_gpu_nmf.so from the staged sources; returns its path or None."""
+    root = stage_ref_gpu_sources()
+    if root is None:
+        return None
+    shim = os.path.join(HERE, "ref_gpu_shim.cu")
+    out = os.path.join(REF_DIR, "libref_gpu_nmf.so")
+    srcs = [os.path.join(root, rel) for rel in REF_GPU_FILES if rel.endswith((".cpp", ".cu"))]
+    if not force and _newer(out, [shim, __file__] + srcs):
+        return out
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+           "-Xcompiler", "-fPIC", "-w", *REF_GPU_DEFINES, "-I", os.path.join(root, "src"),
+           shim, *srcs, "-o", out, "-lcublas"]
+    subprocess.run(cmd, check=True)
+    return out
+
+
 def stage_faces_images():
     """Copy the FacesNMF data set into oracle/_ref/faces_images/; returns the folder or None."""
     src = os.path.join(REFERENCE_ROOT, "src/examples/FacesNMF/images")
@@ -186,3 +245,4 @@ if __name__ == "__main__":
     print(build_ref(force="--force" in sys.argv))
     print(build_ref_faces(force="--force" in sys.argv))
     print(stage_faces_images())
+    print(build_ref_gpu(force="--force" in sys.argv))
