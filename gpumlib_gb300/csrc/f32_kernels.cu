@@ -264,23 +264,37 @@ static TileKind pick_tile(int M, int N) {
 static TileDims tile_dims(TileKind t) {
     switch (t) {
         case kSkinnyM32: return {32, 128, 16};
-        case kSkinnyM64: return {64, 128, 16};
+        case kSkinnyM64: return {64, 64, 16};   // 64 threads, 8 x 8 per thread
         case kSkinnyN32: return {128, 32, 16};
-        case kSkinnyN64: return {128, 64, 16};
+        case kSkinnyN64: return {64, 64, 16};
         case kSmall: return {64, 64, 16};
         default: return {128, 128, 8};
     }
 }
 
+// Split-K count.  The long-K products (W'V, VH', their KL forms) have few output tiles, so K is
+// split; what bounds them is the busiest SM: (CTAs on it) x (K per slice).  The count that
+// minimises that, with at least four CTAs per SM counted (fewer do not keep an SM busy), is
+// taken, the smallest among those within 1% of the least.  At 8192 x 8192, r = 64 this is 19
+// slices (2432 CTAs of 64 x 64, 16 per SM): 233 us for W'V against 311 us with 5 slices.
 static int splits_for(int M, int N, int K, TileDims d) {
-    long long tiles = (long long)ceil_div(M, d.bm) * ceil_div(N, d.bn);
-    const long long target = 2LL * kNumSMsGB300;  // two resident CTAs per SM
-    if (tiles >= target) return 1;
-    int s = (int)((target + tiles - 1) / tiles);
+    const long long tiles = (long long)ceil_div(M, d.bm) * ceil_div(N, d.bn);
+    if (tiles >= 4LL * kNumSMsGB300) return 1;
     int maxs = K / 256;  // keep at least 256 of K per slice
-    if (s > maxs) s = maxs;
-    if (s < 1) s = 1;
-    return s;
+    if (maxs < 1) return 1;
+    if (maxs > 64) maxs = 64;
+    auto cost = [&](int s) {
+        long long kc = (long long)ceil_div(ceil_div(K, s), d.bk) * d.bk;
+        long long ctas = tiles * ceil_div(K, kc);
+        long long per_sm = (ctas + kNumSMsGB300 - 1) / kNumSMsGB300;
+        if (per_sm < 4) per_sm = 4;
+        return per_sm * kc;
+    };
+    long long least = cost(1);
+    for (int s = 2; s <= maxs; s++) least = cost(s) < least ? cost(s) : least;
+    for (int s = 1; s <= maxs; s++)
+        if (cost(s) * 100 <= least * 101) return s;
+    return 1;
 }
 
 int gemm_f32_splits(int M, int N, int K) { return splits_for(M, N, K, tile_dims(pick_tile(M, N))); }
@@ -295,9 +309,9 @@ static cudaError_t launch_tiled(TileKind t, int M, int N, int K, int splits, LA 
     dim3 grid(ceil_div(M, d.bm), ceil_div(N, d.bn), splits);
     switch (t) {
         case kSkinnyM32: gemm_f32_kernel<32, 128, 16, 4, 4, LA, LB, Epi><<<grid, 256, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
-        case kSkinnyM64: gemm_f32_kernel<64, 128, 16, 4, 8, LA, LB, Epi><<<grid, 256, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
+        case kSkinnyM64:
+        case kSkinnyN64: gemm_f32_kernel<64, 64, 16, 8, 8, LA, LB, Epi><<<grid, 64, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
         case kSkinnyN32: gemm_f32_kernel<128, 32, 16, 4, 4, LA, LB, Epi><<<grid, 256, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
-        case kSkinnyN64: gemm_f32_kernel<128, 64, 16, 8, 4, LA, LB, Epi><<<grid, 256, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
         case kSmall: gemm_f32_kernel<64, 64, 16, 4, 4, LA, LB, Epi><<<grid, 256, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
         default: gemm_f32_kernel<128, 128, 8, 8, 8, LA, LB, Epi><<<grid, 256, 0, s>>>(M, N, K, kchunk, la, lb, epi); break;
     }
