@@ -71,6 +71,7 @@ SIGNATURES = [
                                             ctypes.POINTER(ctypes.c_void_p)]),
     ("gpunmf_server_submit", ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong] + [ctypes.c_int] * 4 +
      [ctypes.c_ulonglong, ctypes.c_float]),
+    ("gpunmf_server_set_grid_policy", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     ("gpunmf_server_poll", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("gpunmf_server_fetch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),

@@ -183,7 +183,8 @@ static void job_free(gpunmf_job *j) {
 }
 
 static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int precision, void *stream,
-                               gpunmf_job **out, unsigned char *pinned64 = nullptr, bool async_alloc = false) {
+                               gpunmf_job **out, unsigned char *pinned64 = nullptr, bool async_alloc = false,
+                               int cta_cap = 0) {
     *out = nullptr;
     if (!rule_valid(rule)) {
         set_error("unknown rule %d", rule);
@@ -215,6 +216,7 @@ static gpunmf_status job_alloc(int rule, int n, int m, int r, float eps, int pre
         set_error("host allocation failed");
         return GPUNMF_ERR_NOMEM;
     }
+    j->cta_cap = cta_cap > 0 ? cta_cap : 0;
     j->rule = rule; j->n = n; j->m = m; j->r = r; j->eps = eps; j->precision = precision;
     j->async_alloc = async_alloc && stream != nullptr;
     if (stream) {
@@ -470,8 +472,8 @@ static gpunmf_status ensure_wh(gpunmf_job *j) {
 }
 
 gpunmf_status job_create_empty(int rule, int n, int m, int r, float eps, int precision, cudaStream_t stream,
-                               unsigned char *pinned64, bool async_alloc, gpunmf_job **out) {
-    return job_alloc(rule, n, m, r, eps, precision, (void *)stream, out, pinned64, async_alloc);
+                               unsigned char *pinned64, bool async_alloc, gpunmf_job **out, int cta_cap) {
+    return job_alloc(rule, n, m, r, eps, precision, (void *)stream, out, pinned64, async_alloc, cta_cap);
 }
 
 gpunmf_status job_prepare(gpunmf_job *j) {

@@ -12,6 +12,7 @@ struct TcState;  // tensor-core path state (tc_kernels.cu)
 struct gpunmf_job {
     int rule = 0, n = 0, m = 0, r = 0, precision = 0;
     float eps = 1e-8f;
+    int cta_cap = 0;  // CTAs per launch of the tensor-core kernels at most (0: the SMs)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
 
@@ -71,7 +72,7 @@ void job_dev_free(gpunmf_job *j, void *p);
 cudaError_t job_h2d(gpunmf_job *j, void *dst, const void *src, size_t bytes);
 // a job without data (the caller fills V, W, H on the job's stream, then calls job_prepare)
 gpunmf_status job_create_empty(int rule, int n, int m, int r, float eps, int precision, cudaStream_t stream,
-                               unsigned char *pinned64, bool async_alloc, gpunmf_job **out);
+                               unsigned char *pinned64, bool async_alloc, gpunmf_job **out, int cta_cap = 0);
 gpunmf_status job_prepare(gpunmf_job *j);
 gpunmf_status job_run(gpunmf_job *j, int iters, bool updateW);
 void job_release(gpunmf_job *j);  // frees without synchronising (stream-ordered when async_alloc)

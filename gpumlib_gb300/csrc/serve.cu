@@ -18,6 +18,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -104,8 +105,20 @@ struct SJob {
     std::vector<float> W, H;  // kept factors (keep_factors mode)
 };
 
+// CTAs per launch of a served BF16 job's tensor-core kernels: its 128 x 128 blocks per half-step
+// divided by kServeBlocksPerCta, at least one and at most kServeMaxJobCtas.  A job created alone
+// takes one CTA per block up to every SM; in the server the large jobs' grids are capped so that
+// they leave SMs to the jobs running beside them.  Measured on the 2000 jobs/s stream (1 s of it,
+// 1970 jobs, 64 slots): every SM 155 jobs/s, at most 48 CTAs 249, 24 CTAs 306, 12 CTAs 118 (the
+// large jobs then take too long); more than one block per CTA costs more per job than the
+// concurrency gains (8 blocks per CTA: 23 jobs/s), since the kernels are built for about one
+// block per CTA.
+constexpr int kServeBlocksPerCta = 1;
+constexpr int kServeMaxJobCtas = 24;
+
 struct gpunmf_server {
     int device = 0;
+    std::atomic<int> blocks_per_cta{kServeBlocksPerCta}, max_job_ctas{kServeMaxJobCtas};
     int slots = 0, precision = 0, check_every = 10, max_iters = 500;
     size_t budget = 0, in_use = 0;
     double tol = 1e-3;
@@ -183,8 +196,14 @@ static gpunmf_status start_job(gpunmf_server *S, SJob *q) {
     if (prec == GPUNMF_BF16 && tc_supported(q->res.rule, q->res.n, q->res.m, q->res.r) != GPUNMF_OK)
         prec = GPUNMF_FP32;  // the tensor-core path does not cover this job: plain FP32
     q->res.precision = prec;
+    int cap = 0;  // per-job CTA cap of the tensor-core kernels (0: every SM)
+    const int bpc = S->blocks_per_cta.load();
+    if (prec == GPUNMF_BF16 && bpc > 0) {
+        const long long blocks = (long long)ceil_div(q->res.n, 128) * ceil_div(q->res.m, 128);
+        cap = (int)std::min<long long>(std::max(1, S->max_job_ctas.load()), std::max<long long>(1, (blocks + bpc - 1) / bpc));
+    }
     gpunmf_status st = job_create_empty(q->res.rule, q->res.n, q->res.m, q->res.r, q->eps, prec,
-                                        S->streams[q->slot], S->h_pin + 64 * q->slot, true, &q->job);
+                                        S->streams[q->slot], S->h_pin + 64 * q->slot, true, &q->job, cap);
     if (st != GPUNMF_OK) return st;
     q->job->q_interval = 0;
     st = generate_job_data(q->job, q->seed, S->sigma);
@@ -341,6 +360,16 @@ gpunmf_status gpunmf_server_create(int slots, size_t hbm_budget_bytes, int preci
     }
     S->worker = std::thread(worker_loop, S);
     *out = S;
+    return GPUNMF_OK;
+}
+
+gpunmf_status gpunmf_server_set_grid_policy(gpunmf_server *S, int blocks_per_cta, int max_job_ctas) {
+    if (!S || blocks_per_cta < 0 || max_job_ctas < 0) {
+        set_error("invalid grid policy");
+        return GPUNMF_ERR_INVALID;
+    }
+    S->blocks_per_cta.store(blocks_per_cta);
+    S->max_job_ctas.store(max_job_ctas > 0 ? max_job_ctas : kServeMaxJobCtas);
     return GPUNMF_OK;
 }
 

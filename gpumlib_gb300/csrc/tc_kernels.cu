@@ -1949,9 +1949,11 @@ __global__ void __launch_bounds__(kKlThreads)
     } else if (warp == 1) {
         griddep_wait();
         griddep_launch_dependents();
-        // The whole warp runs the MMA loop (its state is warp-uniform, barrier tests are voted), and
-        // one elected lane issues the products and commits: the issue path stays on warp-uniform
-        // values instead of a single divergent lane.
+        // The MMA warp issues in a fixed order: MMA1 of the first nb blocks, then for every block j
+        // MMA2(j) once its R is in TMEM, then MMA1(j + nb) into the S/R buffer MMA2(j) read, once
+        // that MMA2 has completed.  Each step waits on the one barrier it needs, so a product is
+        // issued as soon as its inputs are there.  The whole warp runs the loop (waits are voted),
+        // one elected lane issues the products and commits.
         const uint32_t id1 = idesc_bf16_f32(kTileM, kKlBlockK);
         const uint32_t id2 = idesc_bf16_f32(kTileM, NP) | kIdescBMnMajor;
         // descriptors of A1 and of F stage 0 (K-major for MMA1, MN-major for MMA2: the factor's
@@ -1964,57 +1966,36 @@ __global__ void __launch_bounds__(kKlThreads)
         // blocks of this CTA counted from 0; a segment ends at a tile boundary
         const int nblk = (int)(hi - lo);
         auto seg_end_local = [&](int j) { return (int)(seg_end(lo + j) - lo); };
+        // spin on the barrier: the MMA warp's reaction is on the critical chain, and a sleeping
+        // try_wait resumed a few hundred ns after the phase completed; the error word and the time
+        // limit are checked now and then
+        auto wait = [&](uint64_t *bar, uint32_t parity, int bit) {
+            long long t0 = 0;
+            for (int spin = 1;; spin++) {
+                if (__all_sync(0xffffffffu, mbar_test(bar, parity))) return true;
+                if ((spin & 63) == 0) {
+                    if (__any_sync(0xffffffffu, *((volatile int *)p.err) != 0)) return false;
+                    const long long now = __shfl_sync(0xffffffffu, clock64(), 0);
+                    if (t0 == 0) {
+                        t0 = now;
+                    } else if (now - t0 > p.wait_limit) {
+                        if (leader) atomicOr(p.err, bit);
+                        return false;
+                    }
+                }
+            }
+        };
         // MMA1 cursor: block j1, its F-ring entry and S/R buffer; need_a1: the next entry is the A1
         // of a new segment (each segment's entries are its A1, then one F per block)
         int j1 = 0, e1 = seg_end_local(0), f1 = 0, d1 = 0;
         uint32_t f1ph = 0, d1ph = 0;
         bool need_a1 = true;
-        // MMA2 cursor (starts past the first segment's A1 entry)
-        int j2 = 0, e2 = e1, f2 = 0, d2 = 0, seg2 = 0;
-        uint32_t f2ph = 0, d2ph = 0;
-        ring_next(f2, f2ph, p.sf);
-        bool first2 = true;
-        long long t_idle = 0;
-        int spins = 0;
-        while (j2 < nblk) {
-            bool did = false;
-            // MMA2 of the oldest block whose R is in TMEM (frees its F stage and S/R buffer)
-            if (j2 < j1 && __all_sync(0xffffffffu, mbar_test(&rfull[d2], d2ph))) {
-                // the accumulator of a new segment: the previous segment's numerator drained
-                if (first2 && seg2 > 0 &&
-                    !__all_sync(0xffffffffu, mbar_wait(tempty, (uint32_t)((seg2 - 1) & 1), p.err, kErrWaitTmemEmpty,
-                                                       p.wait_limit)))
-                    break;
-                if (leader) {
-                    tc_fence_after();
-                    const uint64_t fb = fdm + (uint64_t)(f2 * fstep);
-                    const uint32_t rb = tD1 + (uint32_t)(d2 * kKlBlockK);
-#pragma unroll
-                    for (int k = 0; k < kKlBlockK / 16; k++)  // R of part p at columns 32p .. 32p + 15
-                        tc_mma_f16_ts(tD2, rb + (uint32_t)((k >> 1) * 32 + (k & 1) * 8), fb + (uint64_t)(k * 2048 >> 4),
-                                      id2, (first2 && k == 0) ? 0u : 1u);
-                    tc_commit(&fempty[f2]);
-                    tc_commit(&d1empty[d2]);
-                    if (j2 + 1 == e2) tc_commit(tfull);
-                }
-                __syncwarp();
-                first2 = false;
-                ring_next(f2, f2ph, p.sf);
-                ring_next(d2, d2ph, p.nb);
-                if (++j2 == e2) {
-                    seg2++;
-                    first2 = true;
-                    if (j2 < nblk) {
-                        e2 = seg_end_local(j2);
-                        ring_next(f2, f2ph, p.sf);  // past the next segment's A1 entry
-                    }
-                }
-                did = true;
-            }
-            // A1 of a new segment: copied from its F-ring entry into TMEM.  The copy is ordered after
-            // the previous segment's MMA1s (which read the old A1) and before the new ones, like
-            // another MMA of this thread; the entry is freed when it has completed.
-            if (j1 < nblk && need_a1 && __all_sync(0xffffffffu, mbar_test(&ffull[f1], f1ph))) {
+        // MMA1 of block j1; at a segment start the segment's A1 is copied from its F-ring entry into
+        // TMEM first (ordered after the previous segment's MMA1s, which read the old A1, and before
+        // the new ones; the entry is freed when the copy has completed)
+        auto mma1 = [&]() -> bool {
+            if (need_a1) {
+                if (!wait(&ffull[f1], f1ph, kErrWaitFull)) return false;
                 if (leader) {
                     tc_fence_after();
                     const uint64_t ad = fdk + (uint64_t)(f1 * fstep);
@@ -2028,49 +2009,66 @@ __global__ void __launch_bounds__(kKlThreads)
                 __syncwarp();
                 ring_next(f1, f1ph, p.sf);
                 need_a1 = false;
-                did = true;
             }
-            // MMA1 of the next block once its F tile and a free S/R buffer are there
-            if (j1 < nblk && !need_a1) {
-                if (__all_sync(0xffffffffu, mbar_test(&ffull[f1], f1ph) && mbar_test(&d1empty[d1], d1ph ^ 1))) {
-                    if (leader) {
-                        tc_fence_after();
-                        const uint64_t fb = fdk + (uint64_t)(f1 * fstep);
-                        const uint32_t dd = tD1 + (uint32_t)(d1 * kKlBlockK);
+            // the block's F tile, and its S/R buffer free (MMA2 of the block nb earlier completed)
+            if (!wait(&ffull[f1], f1ph, kErrWaitFull) || !wait(&d1empty[d1], d1ph ^ 1, kErrWaitTmemEmpty))
+                return false;
+            if (leader) {
+                tc_fence_after();
+                const uint64_t fb = fdk + (uint64_t)(f1 * fstep);
+                const uint32_t dd = tD1 + (uint32_t)(d1 * kKlBlockK);
 #pragma unroll
-                        for (int k16 = 0; k16 < NK; k16++) {
-                            const int offf = (k16 >> 2) * kKlFBox + (k16 & 3) * 32;
-                            tc_mma_f16_ts(dd, tA1 + (uint32_t)(k16 * 8), fb + (uint64_t)(offf >> 4), id1, k16 > 0 ? 1u : 0u);
-                        }
-                        tc_commit(&d1full[d1]);
-                    }
-                    __syncwarp();
-                    ring_next(f1, f1ph, p.sf);
-                    ring_next(d1, d1ph, p.nb);
-                    if (++j1 == e1) {
-                        need_a1 = true;
-                        if (j1 < nblk) e1 = seg_end_local(j1);
-                    }
-                    did = true;
+                for (int k16 = 0; k16 < NK; k16++) {
+                    const int offf = (k16 >> 2) * kKlFBox + (k16 & 3) * 32;
+                    tc_mma_f16_ts(dd, tA1 + (uint32_t)(k16 * 8), fb + (uint64_t)(offf >> 4), id1, k16 > 0 ? 1u : 0u);
+                }
+                tc_commit(&d1full[d1]);
+            }
+            __syncwarp();
+            ring_next(f1, f1ph, p.sf);
+            ring_next(d1, d1ph, p.nb);
+            if (++j1 == e1) {
+                need_a1 = true;
+                if (j1 < nblk) e1 = seg_end_local(j1);
+            }
+            return true;
+        };
+        bool ok = true;
+        for (int q = 0; q < p.nb && j1 < nblk && ok; q++) ok = mma1();
+        // MMA2 cursor (starts past the first segment's A1 entry)
+        int j2 = 0, e2 = seg_end_local(0), f2 = 0, d2 = 0, seg2 = 0;
+        uint32_t f2ph = 0, d2ph = 0;
+        ring_next(f2, f2ph, p.sf);
+        bool first2 = true;
+        while (ok && j2 < nblk) {
+            if (!wait(&rfull[d2], d2ph, kErrWaitTmemFull)) break;
+            // the accumulator of a new segment: the previous segment's numerator drained
+            if (first2 && seg2 > 0 && !wait(tempty, (uint32_t)((seg2 - 1) & 1), kErrWaitTmemEmpty)) break;
+            if (leader) {
+                tc_fence_after();
+                const uint64_t fb = fdm + (uint64_t)(f2 * fstep);
+                const uint32_t rb = tD1 + (uint32_t)(d2 * kKlBlockK);
+#pragma unroll
+                for (int k = 0; k < kKlBlockK / 16; k++)  // R of part p at columns 32p .. 32p + 15
+                    tc_mma_f16_ts(tD2, rb + (uint32_t)((k >> 1) * 32 + (k & 1) * 8), fb + (uint64_t)(k * 2048 >> 4),
+                                  id2, (first2 && k == 0) ? 0u : 1u);
+                tc_commit(&fempty[f2]);
+                tc_commit(&d1empty[d2]);
+                if (j2 + 1 == e2) tc_commit(tfull);
+            }
+            __syncwarp();
+            first2 = false;
+            ring_next(f2, f2ph, p.sf);
+            ring_next(d2, d2ph, p.nb);
+            if (++j2 == e2) {
+                seg2++;
+                first2 = true;
+                if (j2 < nblk) {
+                    e2 = seg_end_local(j2);
+                    ring_next(f2, f2ph, p.sf);  // past the next segment's A1 entry
                 }
             }
-            if (did) {
-                spins = 0;
-                t_idle = 0;
-            } else if (++spins & 255) {
-                // idle: back off a little, leaving this SM sub-partition's issue slots to the ratio
-                // warps that share it (a wake-up costs at most the back-off)
-                __nanosleep(32);
-            } else {  // now and then: the error word and the time limit
-                if (__any_sync(0xffffffffu, *((volatile int *)p.err) != 0)) break;
-                const long long now = __shfl_sync(0xffffffffu, clock64(), 0);
-                if (t_idle == 0) {
-                    t_idle = now;
-                } else if (now - t_idle > p.wait_limit) {
-                    if (leader) atomicOr(p.err, kErrWaitFull);
-                    break;
-                }
-            }
+            if (j1 < nblk) ok = mma1();
         }
         if (leader) {
             tc_commit(mdone);
@@ -3183,6 +3181,7 @@ gpunmf_status tc_create(gpunmf_job *j) {
     {
         const int cap = g_grid_limit.load();
         t->max_ctas = std::min(num_sms(), cap > 0 ? cap : INT_MAX);
+        if (j->cta_cap > 0) t->max_ctas = std::min(t->max_ctas, j->cta_cap);
     }
     t->npr = (n + 127) / 128 * 128;
     t->mpr = (m + 127) / 128 * 128;

@@ -30,7 +30,7 @@ PRECISIONS = {"fp32": 0, "bf16": 1}
 
 class Server:
     def __init__(self, slots=64, hbm_budget_gb=150.0, precision="bf16", check_every=10, tol=1e-3, max_iters=500,
-                 keep_factors=False):
+                 keep_factors=False, grid_policy=None):
         self._lib = _native.load()
         h = ctypes.c_void_p()
         _native.check(self._lib.gpunmf_server_create(int(slots), int(hbm_budget_gb * (1 << 30)),
@@ -38,6 +38,8 @@ class Server:
                                                      int(max_iters), 1 if keep_factors else 0, ctypes.byref(h)))
         self._h = h
         self.keep = keep_factors
+        if grid_policy is not None:   # (blocks per CTA, max CTAs per job); see gpunmf_server_set_grid_policy
+            _native.check(self._lib.gpunmf_server_set_grid_policy(self._h, int(grid_policy[0]), int(grid_policy[1])))
 
     def submit(self, job_id, rule, n, m, r, seed, eps=1e-9):
         _native.check(self._lib.gpunmf_server_submit(self._h, int(job_id), int(rule), int(n), int(m), int(r),

@@ -323,6 +323,12 @@ gpunmf_status gpunmf_server_create(int slots, size_t hbm_budget_bytes, int preci
                                    double tol, int max_iters, int keep_factors, gpunmf_server **out);
 gpunmf_status gpunmf_server_submit(gpunmf_server *s, long long id, int rule, int n, int m, int r,
                                    unsigned long long seed, float eps);
+/* CTAs per launch of each admitted BF16 job's tensor-core kernels: ceil(blocks / blocks_per_cta),
+ * at least 1 and at most max_job_ctas, where blocks = ceil(n/128) ceil(m/128).  Capping the large
+ * jobs' grids lets more jobs share the SMs at once.  blocks_per_cta 0: every job may use every SM
+ * (as a job created alone does); max_job_ctas 0: the default cap.  Applies to jobs admitted after
+ * the call.  Defaults: 1 block per CTA, at most 24 CTAs. */
+gpunmf_status gpunmf_server_set_grid_policy(gpunmf_server *s, int blocks_per_cta, int max_job_ctas);
 /* Move up to `cap` finished results into out[]; returns their number. */
 int gpunmf_server_poll(gpunmf_server *s, gpunmf_server_result *out, int cap);
 gpunmf_status gpunmf_server_fetch(gpunmf_server *s, long long id, gpunmf_server_result *res, float *W, float *H);

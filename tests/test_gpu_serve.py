@@ -48,6 +48,24 @@ def test_result_alone_equals_result_in_mix(gpu, precision):
         assert any(rs[k + 1]["t_admit"] < rs[k]["t_done"] for k in range(len(rs) - 1))
 
 
+def test_grid_policy_changes_no_result_beyond_rounding(gpu):
+    """The server's per-job CTA cap (gpunmf_server_set_grid_policy) changes only the kernels' stream-K
+    partition, hence FP32 summation orders: same iterations, residuals within 1e-4 relative."""
+    jobs = [dict(id=1, rule=0, n=1500, m=1300, r=48, seed=31), dict(id=2, rule=1, n=900, m=1100, r=32, seed=32)]
+    out = {}
+    for pol in ((0, 0), (1, 5)):
+        with serve.Server(slots=4, precision="bf16", check_every=10, max_iters=40, keep_factors=True,
+                          grid_policy=pol) as s:
+            for j in jobs:
+                s.submit(j["id"], j["rule"], j["n"], j["m"], j["r"], j["seed"])
+            assert s.drain(120)
+            out[pol] = [s.fetch(j["id"], j["n"], j["m"], j["r"]) for j in jobs]
+    for (ra, Wa, Ha), (rb, Wb, Hb) in zip(out[(0, 0)], out[(1, 5)]):
+        assert ra["status"] == 0 and rb["status"] == 0 and ra["iters"] == rb["iters"]
+        assert abs(ra["residual"] - rb["residual"]) <= 1e-4 * ra["residual"]
+        assert rel(Wb.astype(np.float64) @ Hb, Wa.astype(np.float64) @ Ha) <= 5e-3
+
+
 def test_admission_respects_hbm_budget(gpu):
     from gpumlib_gb300 import nmf
     jobs = [dict(id=k, rule=0, n=1024, m=1024, r=32, seed=50 + k) for k in range(6)]
