@@ -280,7 +280,7 @@ static TileDims tile_dims(TileKind t) {
 static int splits_for(int M, int N, int K, TileDims d) {
     const long long tiles = (long long)ceil_div(M, d.bm) * ceil_div(N, d.bn);
     if (tiles >= 4LL * kNumSMsGB300) return 1;
-    int maxs = K / 256;  // keep at least 256 of K per slice
+    int maxs = K / 64;  // keep at least 64 of K per slice
     if (maxs < 1) return 1;
     if (maxs > 64) maxs = 64;
     auto cost = [&](int s) {
@@ -323,6 +323,9 @@ static cudaError_t gemm_store(int M, int N, int K, LA la, LB lb, float *C, long 
                               cudaStream_t s) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     TileKind t = pick_tile(M, N);
+    // short K (the Gram-times-factor products, K = r): the same 64 x 64 tiles with 4 x 4 outputs per
+    // thread, four times the warps to hide the loads
+    if (K <= 128 && (t == kSkinnyM64 || t == kSkinnyN64)) t = kSmall;
     if (splits < 1) splits = 1;
     EpiStore e{C, splits == 1 ? ldc : (long long)M, splits == 1 ? 0LL : (long long)M * N};
     return launch_tiled(t, M, N, K, splits, la, lb, e, s);
