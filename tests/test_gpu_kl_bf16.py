@@ -71,6 +71,26 @@ def test_kl_tiny_eps_matches_emulation(gpu, shape):
     assert rel(W1g, W1) <= 2e-5, "W-step (fused KL tcgen05) differs"
 
 
+@pytest.mark.parametrize("shape", [(1500, 900, 128), (1024, 700, 40)], ids=["1500x900r128", "1024x700r40"])
+def test_kl_sparse_counts_match_emulation(gpu, shape):
+    """Count data with ~90% zeros (the sparse count workload: lambda = 0.01 P Q with P, Q ~ Gamma(0.3, 1)):
+    most ratios V / (S + eps) are exactly 0, the rest large; one iteration against the emulation."""
+    n, m, r = shape
+    g = np.random.Generator(np.random.PCG64(5 * n + m))
+    P = g.gamma(0.3, 1.0, size=(n, 64))
+    Q = g.gamma(0.3, 1.0, size=(64, m))
+    V = np.asfortranarray(g.poisson(0.01 * (P @ Q)).astype(np.float32))
+    assert np.mean(V == 0) > 0.8
+    W, H = inputs.factors(290 + n, n, m, r)
+    eps = np.float32(1e-9)
+    with gpu.NMF_MultiplicativeDivergence(V, W, H, eps=eps, precision="bf16", quality_interval=0) as nmf:
+        nmf.DoIteration()
+        W1g, H1g = nmf.GetW(), nmf.GetH()
+    W1, H1 = emulate_kl_one(V, W, H, float(eps), H1g)
+    assert rel(H1g, H1) <= 2e-5, "H-step (fused KL tcgen05) differs"
+    assert rel(W1g, W1) <= 2e-5, "W-step (fused KL tcgen05) differs"
+
+
 def test_kl_bf16_tracks_fp32(gpu):
     n, m, r = 2048, 1536, 64
     g = np.random.Generator(np.random.PCG64(7))
