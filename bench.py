@@ -750,6 +750,7 @@ def run_serving(args, rank, world, local, dist):
             "config": {"workload": "serving_poisson_%g_per_s_%gs" % (args.serve_rate, args.serve_duration),
                        "rate": args.serve_rate, "duration_s": args.serve_duration, "kl_fraction": 0.3,
                        "tol": 1e-3, "max_iters": 500, "hbm_budget_gb": 150, "slots": args.serve_slots,
+                       "grid_policy": "BF16 jobs: one CTA per 128x128 block, at most 24 CTAs (server default)",
                        "drain_timeout_s": args.serve_drain},
             "clocks": clk.summary(), "arms": out_arms,
             "note": "one_job_at_a_time_fp32 replays the first 5% of the trace through a single slot"}
