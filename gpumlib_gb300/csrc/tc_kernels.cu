@@ -129,6 +129,10 @@ __device__ __forceinline__ bool epi_bar_or(bool v) {
 // denominator, a 64-row staging tile, a flag word and the slot lists of two tiles.
 constexpr int kFusedSlots = 15;  // slots per tile the fused update handles (more: the separate update kernel)
 __host__ __device__ constexpr int fused_gram_floats(int np) { return np * np > 64 * np ? np * np : 64 * np; }
+// Per-CTA Gram partials are stored packed: entry (i, k), i <= k, at k (k + 1) / 2 + i, a partial every
+// tri_stride(np) floats.  The CTA that sums entries [u0, u1) of every partial then reads one contiguous
+// run of each.
+__host__ __device__ constexpr int tri_stride(int np) { return (np * (np + 1) / 2 + 3) / 4 * 4; }
 __host__ __device__ constexpr int fused_smem_bytes(int np) {
     // the Gram area also holds a chunk's denominators (64 x np)
     return np == 0 ? 0 : fused_gram_floats(np) * 4 + 64 * (np + 4) * 4 + 16 + 2 * (kFusedSlots + 1) * 4 + 64;
@@ -292,10 +296,11 @@ __device__ __forceinline__ int2 tri_entry(int u) {
 // Prologue of the fused update (the two worker warps, while V streams).  The complete Gram of the
 // other factor is assembled from that factor's per-CTA partials: this CTA sums a slice of the
 // upper triangle over the partials in their order (so the result does not depend on which CTA
-// does it) and writes both mirror entries.  Entry (i, k), i <= k, is read at k * NP + i: every
-// partial is exactly symmetric (the same products in the same row order), and a slice's entries
-// of one column are then adjacent, so a warp's loads of one partial share sectors; once every CTA has published its slice (grid-wide
-// counter, bounded wait) the whole Gram is copied in.  Meanwhile the old rows of this CTA's first
+// does it) and writes both mirror entries.  The partials are packed (tri_stride), so this CTA's
+// slice of one partial is one contiguous run and a warp's loads of it share sectors (the run was
+// scattered over the partial's columns before: 8.7 us for this phase at 8192 x 8192, r = 64, under
+// the V stream); once every CTA has published its slice (grid-wide counter, bounded wait) the
+// whole Gram is copied in.  Meanwhile the old rows of this CTA's first
 // chunk are copied in; then the chunk's denominators (left in sG as sD).  All copies are
 // cp.async, so they are in flight together while the stream holds HBM.
 template <int NP>
@@ -311,8 +316,7 @@ __device__ __forceinline__ void fused_prologue(const SkParams &pr, int wt, float
         const int nb = min(per, u1 - ub);
         for (int k = wt; k < nb * P; k += 64) {  // sG[q * nb + j]: entry ub + j of partial q
             const int q = k / nb, j = k - q * nb;
-            const int2 ik = tri_entry(ub + j);
-            cp_async4(sG + k, pr.gin_parts + (size_t)q * E + ik.y * NP + ik.x, true);
+            cp_async4(sG + k, pr.gin_parts + (size_t)q * tri_stride(NP) + ub + j, true);
         }
         cp_async_commit();
         cp_async_wait_all();
@@ -378,7 +382,7 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
     const long long x0 = (long long)c * rows / G, x1 = (long long)(c + 1) * rows / G;
     const int a0 = (tid % L::AG) * L::APT, r0 = (tid / L::AG) * L::RPT;
     const int ga0 = (tid / TB) * GB, gb0 = (tid % TB) * GB2;
-    float *const gpc = pr.gp + (size_t)c * E;
+    float *const gpc = pr.gp + (size_t)c * tri_stride(NP);
     const float *sD = sG;
     auto bar = [] { tail_sync<NT, SUBSET>(); };
     float gacc[GB][GB2];
@@ -530,20 +534,17 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
             }
         }
     }
-    // the next launch reads entry (i, k), i <= k, at k * NP + i: only blocks that reach that triangle
-    // are written, GB values at a time
+    // this CTA's partial, packed (tri_stride): the thread's block holds G(ga, gb) for ga in
+    // [ga0, ga0 + GB), gb in [gb0, gb0 + GB2); those with gb <= ga are entry (gb, ga), at
+    // ga (ga + 1) / 2 + gb
     if (ga0 + GB - 1 >= gb0) {
 #pragma unroll
         for (int i = 0; i < GB; i++) {
-            float *dst = gpc + (ga0 + i) * NP + gb0;
-            if constexpr (GB2 == 4) {
-                *reinterpret_cast<float4 *>(dst) = make_float4(gacc[i][0], gacc[i][1], gacc[i][2], gacc[i][3]);
-            } else if constexpr (GB2 == 2) {
-                *reinterpret_cast<float2 *>(dst) = make_float2(gacc[i][0], gacc[i][1]);
-            } else {
+            const int ga = ga0 + i;
+            float *dst = gpc + ga * (ga + 1) / 2;
 #pragma unroll
-                for (int k = 0; k < GB2; k++) dst[k] = gacc[i][k];
-            }
+            for (int k = 0; k < GB2; k++)
+                if (gb0 + k <= ga) dst[gb0 + k] = gacc[i][k];
         }
     }
 }
@@ -572,7 +573,8 @@ __global__ void __launch_bounds__(64) gram_partials_kernel(const float *__restri
             for (int k = 0; k < L::NPT; k++) gacc[k] = fmaf(xa, sX[rr * L::LDX + gb0 + k], gacc[k]);
         }
     }
-    for (int k = 0; k < L::NPT; k++) out[(size_t)c * NP * NP + ga * NP + gb0 + k] = gacc[k];
+    for (int k = 0; k < L::NPT; k++)  // packed (tri_stride): entry (gb, ga), gb <= ga
+        if (gb0 + k <= ga) out[(size_t)c * tri_stride(NP) + ga * (ga + 1) / 2 + gb0 + k] = gacc[k];
 }
 
 // threads of the GEMM: producer, MMA issuer, four TMEM-draining warps, with a fused update two
