@@ -50,8 +50,8 @@ METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
 # DRAM bytes (read + write) per launch of the dominant kernel, from the committed ncu
 # captures of this workload (one --set full capture per precision, see the profiles
 # directory): tc_gemm_sk_kernel<64> with the update fused, mean of an H-step and a W-step launch,
-# 139.36 MB + 3.35 MB; gemm_f32_kernel (W'V, 19 split-K slices) 275.49 MB + 25.29 MB.
-NCU_TRAFFIC_PER_LAUNCH = {"bf16": 142.71e6, "fp32": 300.78e6}
+# 138.76 MB + 3.75 MB; gemm_f32_kernel (W'V, 19 split-K slices) 275.49 MB + 25.29 MB.
+NCU_TRAFFIC_PER_LAUNCH = {"bf16": 142.51e6, "fp32": 300.78e6}
 # The same for the KL workload's fused product (tc_kl_gemm_kernel<8>, mean of an H-step and a
 # W-step launch: 139.87 MB + 3.94 MB).
 KL_NCU_TRAFFIC_PER_LAUNCH = {"bf16": 143.81e6}
