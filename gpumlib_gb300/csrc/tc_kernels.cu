@@ -583,7 +583,11 @@ __host__ __device__ constexpr int gemm_threads(int fnp, bool qf = false) {
     return (fnp ? kGemmThreads + 64 : kGemmThreads) + (qf ? 256 : 0);
 }
 constexpr int kQfWarps = 8;
-constexpr uint32_t kQfTmemS = 128;  // TMEM column of the first of the two 128-column S buffers
+constexpr uint32_t kQfTmemS = 128;  // TMEM column of the first of the 128-column S buffers
+// S buffers (TMEM, 128 columns each, after the two accumulators): three, so that the MMA of a block's S
+// waits for the quality warps' read of the S three blocks back, and the stage that S MMA reads (its W
+// tile) is held that much less (two: the sampling H-step's stream waited on the quality warps)
+constexpr int kQfSBufs = 3;
 
 // The hardware's approximate base-2 logarithm (lg2.approx.ftz.f32): its argument s + eps is at
 // least eps >= 1e-30 (s >= 0), a normal float, so flushing subnormals changes nothing.
@@ -620,8 +624,8 @@ __global__ void __launch_bounds__(gemm_threads(FNP, QF), 1)
     uint64_t *tempty = tfull + 2;        // [2]
     uint64_t *mdone = tempty + 2;        // [1]
     uint64_t *qfull = mdone + 1;         // QF: [2] H tile loaded, [2] free, [2] S ready, [2] S drained
-    uint64_t *qempty = qfull + 2, *sfull = qempty + 2, *sempty = sfull + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(QF ? sempty + 2 : mdone + 1);
+    uint64_t *qempty = qfull + 2, *sfull = qempty + 2, *sempty = sfull + kQfSBufs;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(QF ? sempty + kQfSBufs : mdone + 1);
     // fused-update areas (FNP > 0): Gram, 64-row staging tile, flag
     float *sG = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tmem_slot + 4) + 15) & ~uintptr_t(15));
     float *sX = sG + fused_gram_floats(FNP);
@@ -646,6 +650,10 @@ __global__ void __launch_bounds__(gemm_threads(FNP, QF), 1)
             if constexpr (QF) {
                 mbar_init(&qfull[a], 1);
                 mbar_init(&qempty[a], 1);
+            }
+        }
+        if constexpr (QF) {
+            for (int a = 0; a < kQfSBufs; a++) {
                 mbar_init(&sfull[a], 1);
                 mbar_init(&sempty[a], kQfWarps);
             }
@@ -795,7 +803,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP, QF), 1)
                             tc_mma_f16(tmem + kQfTmemS + (uint32_t)(sb * 128), smem_desc(qa + k16 * 2048, boxB, 1024, 2),
                                        smem_desc(qb + k16 * 2048, boxB, 1024, 2), idesc_q, k16 > 0 ? 1u : 0u);
                         tc_commit(&sfull[sb]);
-                        if (++sb == 2) {
+                        if (++sb == kQfSBufs) {
                             sb = 0;
                             sph ^= 1;
                         }
@@ -960,7 +968,7 @@ __global__ void __launch_bounds__(gemm_threads(FNP, QF), 1)
                 stage = 0;
                 phase ^= 1;
             }
-            if (++sb == 2) {
+            if (++sb == kQfSBufs) {
                 sb = 0;
                 sph ^= 1;
             }
@@ -2545,7 +2553,7 @@ static gpunmf_status setup_gemm(gpunmf_job *j, TcGemm &g, int rows, int K, int n
     g.p.wait_limit = kWaitLimitCycles;
     g.smem = 1024 + stages * stage_bytes + (2 * stages + 5) * 8 + 16 + (fnp ? 16 + fused_smem_bytes(fnp) : 0);
     // with the folded quality sample: two H-tile slots, eight more barriers, the warps' sums
-    g.smem_qf = g.smem + 2 * 2 * npad * kBlockK * 2 + 8 * 8 + 2 * kQfWarps * 8;
+    g.smem_qf = g.smem + 2 * 2 * npad * kBlockK * 2 + (4 + 2 * kQfSBufs) * 8 + 2 * kQfWarps * 8;
     g.fnp = fnp;
     size_t slots = (size_t)g.grid * max_seg;
     cudaError_t e = job_dev_alloc(j, (void **)partials, slots * kTileM * npad * sizeof(float));
