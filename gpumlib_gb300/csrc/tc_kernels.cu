@@ -2238,94 +2238,128 @@ struct KlUpdParams {
     int additive;        // 1: X = max(0, X + (X / max(sum, eps)) (num - sum))
 };
 
-template <int RP, bool IS_W>
+// COLS columns of H (rows of W) per CTA: 8 for the H-step (its m is the smaller side: more CTAs),
+// 16 for the W-step.  The old rows are staged in shared memory (W: read along its columns, H: along
+// the rank), then the numerators are summed with the rank fastest, so the loads of the partial slots
+// ([slot][row][npad]) are coalesced for both factors.
+constexpr int kKlUpdColsH = 8, kKlUpdColsW = 16;
+template <int RP, bool IS_W, int COLS>
 __global__ void __launch_bounds__(kUpdThreads) tc_kl_update_kernel(KlUpdParams p) {
-    constexpr int LDX = kUpdCols + 1;
+    constexpr int LDX = COLS + 1;  // odd: rank-fastest accesses of Xs[a][c] hit distinct banks
+    constexpr int TOT = RP * COLS;  // 128 (r <= 16 in the H-step) up to 2048 elements
+    constexpr int XL = (TOT + kUpdThreads - 1) / kUpdThreads;
     __shared__ float Xs[RP * LDX];
     __shared__ float sumS[RP], sumR[RP];
     const int tid = threadIdx.x;
-    const int c0 = blockIdx.x * kUpdCols;
-    const int ncol = min(kUpdCols, p.cols - c0);
+    const int c0 = blockIdx.x * COLS;
+    const int ncol = min(COLS, p.cols - c0);
     const int r = p.r;
     griddep_wait();
     griddep_launch_dependents();
-    constexpr int XL = RP * kUpdCols / kUpdThreads;
-    float xv[XL], acc[XL];
 #pragma unroll
-    for (int j = 0; j < XL; j++) {
+    for (int j = 0; j < XL; j++) {  // the old rows, zero beyond r and beyond the last column
         const int k = tid + j * kUpdThreads;
+        if (TOT % kUpdThreads != 0 && k >= TOT) break;
         if (IS_W) {
-            const int a = k / kUpdCols, c = k % kUpdCols;
-            xv[j] = (a < r && c < ncol) ? p.X[(long long)a * p.ldx + c0 + c] : 0.f;
+            const int a = k / COLS, c = k % COLS;
+            Xs[a * LDX + c] = (a < r && c < ncol) ? p.X[(long long)a * p.ldx + c0 + c] : 0.f;
         } else {
             const int c = k / RP, a = k % RP;
-            xv[j] = (a < r && c < ncol) ? p.X[(long long)(c0 + c) * r + a] : 0.f;
+            Xs[a * LDX + c] = (a < r && c < ncol) ? p.X[(long long)(c0 + c) * r + a] : 0.f;
         }
-        acc[j] = 0.f;
     }
     if (tid < RP) {
         const float sraw = p.update ? p.sums[tid] : 0.f;
         sumS[tid] = p.update ? fmaxf(sraw, p.eps) : 1.f;
         sumR[tid] = sraw;
     }
-    if (p.update) {
-        const int tile = c0 / 128, lrow0 = c0 % 128;
-        auto add_slot = [&](int sl) {
-            const float *bs = p.P + ((size_t)sl * 128 + lrow0) * p.npad;
+    float acc[XL];
 #pragma unroll
-            for (int j = 0; j < XL; j++) {
-                const int k = tid + j * kUpdThreads;
-                int a, c;
-                if (IS_W) { a = k / kUpdCols; c = k % kUpdCols; }
-                else      { c = k / RP; a = k % RP; }
-                if (c < ncol) acc[j] += bs[c * p.npad + a];
-            }
-        };
+    for (int j = 0; j < XL; j++) acc[j] = 0.f;
+    if (p.update) {  // element (c, a) of thread-slot j: c = k / RP, a = k % RP (rank fastest)
+        // Rows lrow0 + c < 128 of a slot (RP == npad): in bounds for c up to COLS - 1, so the loads
+        // need no column guard (sums over the tile's padding rows are never stored).
+        const int tile = c0 / 128, lrow0 = c0 % 128;
+        int off[XL];
+#pragma unroll
+        for (int j = 0; j < XL; j++) {
+            const int k = tid + j * kUpdThreads;
+            off[j] = (k / RP) * p.npad + k % RP;
+        }
+        auto live = [&](int j) { return TOT % kUpdThreads == 0 || tid + j * kUpdThreads < TOT; };
         if (p.tile_slots) {
+            // the table lists a tile's slots first, then -1: four slots' loads are issued together
+            // (an absent slot reads the first one again and is not added), in slot order as added
             const int4 *ts = reinterpret_cast<const int4 *>(p.tile_slots + (size_t)tile * kSlotW);
             const int4 sa = ts[0], sb = ts[1];
             const int sl[kSlotW] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
 #pragma unroll
-            for (int q = 0; q < kSlotW; q++)
-                if (sl[q] >= 0) add_slot(sl[q]);
-        } else {
-            for (int q = p.slot_ptr[tile]; q < p.slot_ptr[tile + 1]; q++) add_slot(p.slot_list[q]);
-        }
-    }
-    __syncthreads();
+            for (int q0 = 0; q0 < kSlotW; q0 += 4) {
+                if (q0 > 0 && sl[q0] < 0) continue;
+                float v[4][XL];
 #pragma unroll
-    for (int j = 0; j < XL; j++) {
-        const int k = tid + j * kUpdThreads;
-        int a, c;
-        if (IS_W) { a = k / kUpdCols; c = k % kUpdCols; }
-        else      { c = k / RP; a = k % RP; }
-        float x = xv[j];
-        if (p.update && a < r && c < ncol) {
-            if (p.additive) {
-                x = x + (x / sumS[a]) * (acc[j] - sumR[a]);
-                x = x < 0.f ? 0.f : x;
-            } else {
-                x *= (acc[j] / sumS[a]);
+                for (int q = 0; q < 4; q++) {
+                    const int sq = sl[q0 + q] >= 0 ? sl[q0 + q] : sl[0];
+                    const float *bs = p.P + ((size_t)sq * 128 + lrow0) * p.npad;
+#pragma unroll
+                    for (int j = 0; j < XL; j++) v[q][j] = live(j) ? bs[off[j]] : 0.f;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (sl[q0 + q] >= 0) {
+#pragma unroll
+                        for (int j = 0; j < XL; j++) acc[j] += v[q][j];
+                    }
             }
-            if (IS_W) p.X[(long long)a * p.ldx + c0 + c] = x;
-            else p.X[(long long)(c0 + c) * r + a] = x;
+        } else {
+            for (int q = p.slot_ptr[tile]; q < p.slot_ptr[tile + 1]; q++) {
+                const float *bs = p.P + ((size_t)p.slot_list[q] * 128 + lrow0) * p.npad;
+#pragma unroll
+                for (int j = 0; j < XL; j++)
+                    if (live(j)) acc[j] += bs[off[j]];
+            }
         }
-        Xs[a * LDX + c] = x;
     }
     __syncthreads();
     if (p.update) {
-        for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {  // Xb: c fastest
-            const int a = k / kUpdCols, c = k % kUpdCols;
+#pragma unroll
+        for (int j = 0; j < XL; j++) {
+            const int k = tid + j * kUpdThreads, c = k / RP, a = k % RP;
+            if (a < r && c < ncol) {
+                float x = Xs[a * LDX + c];
+                if (p.additive) {
+                    x = x + (x / sumS[a]) * (acc[j] - sumR[a]);
+                    x = x < 0.f ? 0.f : x;
+                } else {
+                    x *= (acc[j] / sumS[a]);
+                }
+                Xs[a * LDX + c] = x;
+            }
+        }
+    }
+    __syncthreads();
+    if (p.update) {
+        for (int k = tid; k < RP * COLS; k += kUpdThreads) {  // X: along W's columns / H's rank
+            if (IS_W) {
+                const int a = k / COLS, c = k % COLS;
+                if (a < r && c < ncol) p.X[(long long)a * p.ldx + c0 + c] = Xs[a * LDX + c];
+            } else {
+                const int c = k / RP, a = k % RP;
+                if (a < r && c < ncol) p.X[(long long)(c0 + c) * r + a] = Xs[a * LDX + c];
+            }
+        }
+        for (int k = tid; k < RP * COLS; k += kUpdThreads) {  // Xb: c fastest
+            const int a = k / COLS, c = k % COLS;
             if (a < r && c < ncol) p.Xb[(long long)a * p.ldb + c0 + c] = __float2bfloat16_rn(Xs[a * LDX + c]);
         }
-        for (int k = tid; k < RP * kUpdCols; k += kUpdThreads) {  // Xr: a fastest
+        for (int k = tid; k < RP * COLS; k += kUpdThreads) {  // Xr: a fastest
             const int c = k / RP, a = k % RP;
             if (c < ncol) p.Xr[(long long)(c0 + c) * p.ldr + a] = __float2bfloat16_rn(a < r ? Xs[a * LDX + c] : 0.f);
         }
     }
     if (tid < RP) {
         float sacc = 0.f;
-        for (int c = 0; c < kUpdCols; c++) sacc += Xs[tid * LDX + c];
+        for (int c = 0; c < COLS; c++) sacc += Xs[tid * LDX + c];
         p.sum_partials[(size_t)blockIdx.x * RP + tid] = sacc;
     }
 }
@@ -2949,7 +2983,7 @@ static cudaError_t launch_kl_gemm(KlGemm &g, cudaStream_t s) {
 
 static cudaError_t launch_kl_update(const KlUpdParams &u, int rp, bool is_w, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(ceil_div(u.cols, kUpdCols));
+    cfg.gridDim = dim3(ceil_div(u.cols, is_w ? kKlUpdColsW : kKlUpdColsH));
     cfg.blockDim = dim3(kUpdThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
@@ -2959,10 +2993,10 @@ static cudaError_t launch_kl_update(const KlUpdParams &u, int rp, bool is_w, cud
     cfg.attrs = at;
     cfg.numAttrs = 1;
     switch (rp) {
-#define CASE(R)                                                                          \
-    case R:                                                                              \
-        return is_w ? cudaLaunchKernelEx(&cfg, tc_kl_update_kernel<R, true>, u)          \
-                    : cudaLaunchKernelEx(&cfg, tc_kl_update_kernel<R, false>, u);
+#define CASE(R)                                                                                  \
+    case R:                                                                                      \
+        return is_w ? cudaLaunchKernelEx(&cfg, tc_kl_update_kernel<R, true, kKlUpdColsW>, u)     \
+                    : cudaLaunchKernelEx(&cfg, tc_kl_update_kernel<R, false, kKlUpdColsH>, u);
         CASE(16) CASE(32) CASE(48) CASE(64) CASE(80) CASE(96) CASE(112) CASE(128)
 #undef CASE
     }
@@ -2999,7 +3033,7 @@ static gpunmf_status tc_create_kl(gpunmf_job *j) {
     TcState *t = j->tc;
     const int n = j->n, m = j->m, r = j->r;
     t->ldr = t->npad;
-    const int cw = ceil_div(n, kUpdCols), ch = ceil_div(m, kUpdCols);
+    const int cw = ceil_div(n, kKlUpdColsW), ch = ceil_div(m, kKlUpdColsH);  // the update kernels' CTAs
     cudaError_t e = job_dev_alloc(j, (void **)&t->Vb, (size_t)t->npr * t->mpr * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Vbt, (size_t)t->npr * t->mpr * 2);
     if (e == cudaSuccess) e = job_dev_alloc(j, (void **)&t->Wb, (size_t)t->ldw * r * 2);
@@ -3171,7 +3205,7 @@ size_t tc_footprint(int rule, int n, int m, int r) {
         size_t b = 2 * (2 * (size_t)((n + 127) / 128 * 128) * ((m + 127) / 128 * 128) + (size_t)ceil8(n) * r +
                         (size_t)ceil8(m) * r + (size_t)(n + m) * npad);
         b += gemm_partial_bytes(m, n, npad) + gemm_partial_bytes(n, m, npad);
-        b += (size_t)npad * sizeof(float) * (2 + ceil_div(n, kUpdCols) + ceil_div(m, kUpdCols)) + 64;
+        b += (size_t)npad * sizeof(float) * (2 + ceil_div(n, kKlUpdColsW) + ceil_div(m, kKlUpdColsH)) + 64;
         return b;
     }
     size_t b = 2 * (2 * (size_t)((n + 127) / 128 * 128) * ((m + 127) / 128 * 128) + (size_t)ceil8(n) * r +
