@@ -318,14 +318,27 @@ static gpunmf_status job_upload(gpunmf_job *j, const float *V, const float *W, c
 }
 
 // ------------------------------------------------------------------------
-// quality bookkeeping (nmf_base.h:70-89), made deterministic: instead of
-// sampling only when the previous asynchronous read-back happens to be
-// complete, the previous read-back is always waited for.
+// quality bookkeeping (nmf_base.h:70-89).  By default made deterministic:
+// instead of sampling only when the previous asynchronous read-back happens to
+// be complete, every k-th iteration samples and the previous read-back is
+// waited for.  Interval GPUNMF_QUALITY_WHEN_READY keeps the reference's own
+// rule: an iteration samples only if the previous read-back is complete
+// (nmf_base.h:71, cudaStreamQuery on the read-back's stream), and never waits.
 // ------------------------------------------------------------------------
 static gpunmf_status quality_step(gpunmf_job *j, bool fused_wh) {
-    if (j->q_interval <= 0 || (j->iter_count % j->q_interval) != 0) return GPUNMF_OK;
+    if (j->q_interval == 0) return GPUNMF_OK;
+    if (j->q_interval > 0 && (j->iter_count % j->q_interval) != 0) return GPUNMF_OK;
     if (j->q_pending) {
-        GPUNMF_CUDA_TRY(cudaEventSynchronize(j->qev));
+        if (j->q_interval == GPUNMF_QUALITY_WHEN_READY) {
+            const cudaError_t e = cudaEventQuery(j->qev);
+            if (e == cudaErrorNotReady) {
+                if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();  // not an error
+                return GPUNMF_OK;
+            }
+            GPUNMF_CUDA_TRY(e);
+        } else {
+            GPUNMF_CUDA_TRY(cudaEventSynchronize(j->qev));
+        }
         j->q_pending = false;
     }
     float quality = j->h_quality()[0];
@@ -627,8 +640,8 @@ gpunmf_status gpunmf_iterate(gpunmf_handle h, int iters, int updateW) {
 
 gpunmf_status gpunmf_set_quality_interval(gpunmf_handle h, int interval) {
     CHECK_HANDLE(h);
-    if (interval < 0) {
-        set_error("interval must be >= 0");
+    if (interval < 0 && interval != GPUNMF_QUALITY_WHEN_READY) {
+        set_error("interval must be >= 0 or GPUNMF_QUALITY_WHEN_READY (-1)");
         return GPUNMF_ERR_INVALID;
     }
     h->q_interval = interval;

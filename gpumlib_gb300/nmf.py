@@ -32,6 +32,9 @@ ADDITIVE_DIVERGENCE = 3
 ADDITIVE_EUCLIDEAN_FIXED_H = 4
 PRECISIONS = {"fp32": 0, "bf16": 1}
 REFERENCE_EPS = np.float32(1e-8)
+# quality_interval / SetQualityInterval: sample only when the previous sample's read-back is complete,
+# never waiting (the reference's rule, nmf_base.h:71); k > 0 samples every k-th iteration, 0 never
+QUALITY_WHEN_READY = -1
 
 
 def _fortran32(a):
@@ -108,6 +111,8 @@ class NMF:
         _native.check(self._lib.gpunmf_iterate(self._h, int(iters), 1 if updateW else 0))
 
     def SetQualityInterval(self, k):
+        """k > 0: sample every k-th iteration (waiting for the previous read-back); 0: never;
+        QUALITY_WHEN_READY: the reference's rule (sample when the previous read-back is complete)."""
         _native.check(self._lib.gpunmf_set_quality_interval(self._h, int(k)))
 
     def Residual(self):

@@ -120,10 +120,16 @@ gpunmf_status gpunmf_iterate(gpunmf_handle h, int iters, int updateW);
 
 /*
  * Quality bookkeeping of DetermineQualityImprovement (nmf_base.h:70-89).
- * interval k > 0: the log10 quality is evaluated every k-th iteration
- * (1 = every iteration, the reference's behaviour when its GPU keeps up);
- * 0 turns it off.  Default: 1.
+ * interval k > 0: the log10 quality is evaluated every k-th iteration, and
+ * each sample first waits for the previous one's read-back (deterministic:
+ * 1 = every iteration, the reference's behaviour when its GPU keeps up);
+ * 0 turns it off; GPUNMF_QUALITY_WHEN_READY is the reference's own rule:
+ * an iteration samples only if the previous sample's read-back has completed
+ * (nmf_base.h:71 queries the read-back's stream), never waiting for it, so
+ * which iterations sample depends on how far the host runs ahead of the GPU.
+ * Default: 1.
  */
+#define GPUNMF_QUALITY_WHEN_READY (-1)
 gpunmf_status gpunmf_set_quality_interval(gpunmf_handle h, int interval);
 
 /*

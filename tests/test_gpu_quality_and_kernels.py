@@ -69,6 +69,48 @@ def test_quality_interval_zero_disables(gpu):
         assert nmf.QualityImprovement() == 1.0
 
 
+@pytest.mark.parametrize("precision,rule", [("fp32", 0), ("fp32", 1), ("bf16", 0), ("bf16", 1)])
+def test_when_ready_with_every_readback_complete_matches_interval_one(gpu, precision, rule):
+    """QUALITY_WHEN_READY (the reference's rule, nmf_base.h:71) samples an iteration only when the
+    previous sample's read-back is complete.  With the host waiting for the job after every iteration
+    every read-back is complete, so it samples every iteration: the same improvements as interval 1
+    and the same factors, bit for bit (sampling never changes the factors)."""
+    n, m, r = 1024, 768, 64
+    V = inputs.lowrank_gamma(n, m, 16, 2.0, 0.5, seed=45)
+    W, H = inputs.factors(46, n, m, r)
+    runs = []
+    for k in (1, gpu.QUALITY_WHEN_READY):
+        with gpu.make(rule, V, W, H, eps=1e-9, precision=precision, quality_interval=k) as nmf:
+            d = []
+            for _ in range(8):
+                nmf.DoIteration()
+                nmf.GetH()   # waits for the job's stream
+                d.append(nmf.QualityImprovement())
+            runs.append((d, nmf.GetW(), nmf.GetH()))
+    (d1, W1, H1), (d2, W2, H2) = runs
+    assert d1 == d2 and d1[2] != 1.0
+    assert np.array_equal(W1, W2) and np.array_equal(H1, H2)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_when_ready_without_waits_keeps_factors(gpu, rule):
+    """Under QUALITY_WHEN_READY with no host waits the iterations that sample depend on timing, but
+    the factors do not: 60 BF16 iterations end with the W and H of a job that never samples, bit for
+    bit, and the improvement read is finite."""
+    n, m, r = 2048, 1536, 64
+    V = inputs.lowrank_gamma(n, m, 16, 2.0, 0.5, seed=47)
+    W, H = inputs.factors(48, n, m, r)
+    out = []
+    for k in (0, gpu.QUALITY_WHEN_READY):
+        with gpu.make(rule, V, W, H, eps=1e-9, precision="bf16", quality_interval=k) as nmf:
+            for _ in range(60):
+                nmf.DoIteration()
+                q = nmf.QualityImprovement()
+            out.append((nmf.GetW(), nmf.GetH(), q))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == 1.0 and np.isfinite(out[1][2])
+
+
 # ---------------------------------------------------------------------------
 # kernel API on device buffers (torch used only to hold device memory)
 # ---------------------------------------------------------------------------
@@ -159,7 +201,7 @@ def test_status_errors_on_gpu(gpu):
     lib = _native.load()
     V = inputs.uniform_matrix(1, 16, 8)
     with gpu.NMF_MultiplicativeEuclidianDistance(V, 2) as nmf:
-        assert lib.gpunmf_set_quality_interval(nmf._h, -1) == 1
+        assert lib.gpunmf_set_quality_interval(nmf._h, -2) == 1
         assert lib.gpunmf_iterate(nmf._h, -3, 1) == 1
     with pytest.raises(ValueError):
         gpu.NMF_MultiplicativeEuclidianDistance(V, np.ones((15, 2), np.float32), np.ones((2, 8), np.float32))
