@@ -364,6 +364,117 @@ __device__ __forceinline__ void tail_sync() {
     else __syncthreads();
 }
 
+// The Gram partial of a chunk at rank 64: the lower triangle of the 64 x 64 block (with its
+// diagonal) split over NT threads (256 or 512) so that no thread forms products above the
+// diagonal.  The 120 off-diagonal 4 x 4 blocks are cut into 4 x 2 pieces (NT = 256) or 2 x 2 pieces
+// (NT = 512); each diagonal block's 10 entries into two pieces of five, all in the last warp: piece
+// s of block d holds the 2 x 2 lower triangle of columns 4d + 2s, 4d + 2s + 1 and the entries
+// (4d + 2, 4d + s), (4d + 3, 4d + s).  With NT = 256 the last warp also takes blocks 112-119 in
+// 2 x 2 pieces.  Every entry is summed over the rows in order, as with any other split.
+template <int NT>
+struct TriGram64 {
+    static_assert(NT == 256 || NT == 512, "rank-64 Gram split");
+    static constexpr int kOffRows = NT == 256 ? 4 : 2;  // rows of an off-diagonal piece (2 columns)
+    bool last;           // the last warp: a diagonal piece (and with NT = 256 a 2 x 2 piece)
+    int ra, cb;          // off-diagonal piece: rows ra.., columns cb, cb + 1
+    int dd, ds;          // diagonal piece: block dd, half ds
+    float off[kOffRows][2];
+    float dg[5];
+    __device__ __forceinline__ static void block_of(int ob, int &bi, int &bj) {  // ob-th block below the diagonal
+        bi = 1;
+        while (bi * (bi + 1) / 2 <= ob) bi++;
+        bj = ob - bi * (bi - 1) / 2;
+    }
+    __device__ __forceinline__ void init(int tid) {
+        const int warp = tid >> 5, lane = tid & 31;
+        last = warp == NT / 32 - 1;
+        int ob, piece, bi, bj;
+        if (NT == 256 && last) {
+            ob = 112 + (lane >> 2);
+            piece = lane & 3;
+        } else {
+            ob = NT == 256 ? tid >> 1 : tid >> 2;
+            piece = NT == 256 ? tid & 1 : tid & 3;
+        }
+        block_of(ob, bi, bj);
+        if (NT == 256 && !last) {
+            ra = 4 * bi;
+            cb = 4 * bj + 2 * piece;
+        } else {
+            ra = 4 * bi + 2 * (piece >> 1);
+            cb = 4 * bj + 2 * (piece & 1);
+        }
+        dd = lane >> 1;
+        ds = lane & 1;
+#pragma unroll
+        for (int i = 0; i < kOffRows; i++) off[i][0] = off[i][1] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 5; i++) dg[i] = 0.f;
+    }
+    // rows [0, nr) of the staged chunk (row stride ldx floats)
+    __device__ __forceinline__ void add_rows(const float *sX, int ldx, int nr) {
+        if (!last) {
+#pragma unroll 4
+            for (int rr = 0; rr < nr; rr++) {
+                float xa[kOffRows], xb[2];
+                lds_vec<kOffRows>(sX + rr * ldx + ra, xa);
+                lds_vec<2>(sX + rr * ldx + cb, xb);
+#pragma unroll
+                for (int i = 0; i < kOffRows; i++) {
+                    off[i][0] = fmaf(xa[i], xb[0], off[i][0]);
+                    off[i][1] = fmaf(xa[i], xb[1], off[i][1]);
+                }
+            }
+        } else {
+            const int c0 = 4 * dd;
+#pragma unroll 4
+            for (int rr = 0; rr < nr; rr++) {
+                const float *row = sX + rr * ldx;
+                float u[2], x23[2];
+                lds_vec<2>(row + c0 + 2 * ds, u);
+                lds_vec<2>(row + c0 + 2, x23);
+                const float w = row[c0 + ds];
+                dg[0] = fmaf(u[0], u[0], dg[0]);
+                dg[1] = fmaf(u[1], u[0], dg[1]);
+                dg[2] = fmaf(u[1], u[1], dg[2]);
+                dg[3] = fmaf(x23[0], w, dg[3]);
+                dg[4] = fmaf(x23[1], w, dg[4]);
+                if constexpr (NT == 256) {
+                    float xa[2], xb[2];
+                    lds_vec<2>(row + ra, xa);
+                    lds_vec<2>(row + cb, xb);
+#pragma unroll
+                    for (int i = 0; i < 2; i++) {
+                        off[i][0] = fmaf(xa[i], xb[0], off[i][0]);
+                        off[i][1] = fmaf(xa[i], xb[1], off[i][1]);
+                    }
+                }
+            }
+        }
+    }
+    // entry (a, b), b <= a, at a (a + 1) / 2 + b of the packed partial
+    __device__ __forceinline__ void store(float *gpc) const {
+        const int nrows = last ? 2 : kOffRows;
+        if (!last || NT == 256) {
+#pragma unroll
+            for (int i = 0; i < kOffRows; i++)
+                if (i < nrows) {
+                    float *dst = gpc + (ra + i) * (ra + i + 1) / 2 + cb;
+                    dst[0] = off[i][0];
+                    dst[1] = off[i][1];
+                }
+        }
+        if (last) {
+            const int a0 = 4 * dd + 2 * ds, c = 4 * dd + ds, a2 = 4 * dd + 2;
+            gpc[a0 * (a0 + 1) / 2 + a0] = dg[0];
+            gpc[(a0 + 1) * (a0 + 2) / 2 + a0] = dg[1];
+            gpc[(a0 + 1) * (a0 + 2) / 2 + a0 + 1] = dg[2];
+            gpc[a2 * (a2 + 1) / 2 + c] = dg[3];
+            gpc[(a2 + 1) * (a2 + 2) / 2 + c] = dg[4];
+        }
+    }
+};
+
 template <int NP, int NT = 256, bool SUBSET = false>
 __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *sG, float *sX, int *sflag, int *sSl) {
     using L = FusedLayout<NP, NT>;
@@ -385,11 +496,13 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
     float *const gpc = pr.gp + (size_t)c * tri_stride(NP);
     const float *sD = sG;
     auto bar = [] { tail_sync<NT, SUBSET>(); };
-    float gacc[GB][GB2];
+    float gacc[GB][GB2];  // other ranks
 #pragma unroll
     for (int i = 0; i < GB; i++)
 #pragma unroll
         for (int k = 0; k < GB2; k++) gacc[i][k] = 0.f;
+    TriGram64<NT> tg;  // rank 64
+    if constexpr (NP == 64) tg.init(tid);
 #pragma unroll 1
     for (long long xb = x0; xb < x1; xb += 64) {
         const int nr = (int)min(64LL, x1 - xb);
@@ -495,33 +608,40 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
                 *reinterpret_cast<float4 *>(sX + (r0 + k) * L::LDX + a0 + 4 * cc) =
                     make_float4(num[k][4 * cc], num[k][4 * cc + 1], num[k][4 * cc + 2], num[k][4 * cc + 3]);
         tail_sync<NT, SUBSET>();
+        // column-order writes (W, and both factors' BF16 copies): a warp step covers 32 rows of four
+        // columns, lane l row l, the column rotating with l / 8 and the step, so the reads of the
+        // staged rows (row stride 4 banks mod 32) fall in 32 distinct banks
 #pragma unroll 4
         for (int kk = 0; kk < L::SL; kk++) {
             const int k = tid + kk * NT;
+            const int lane = k & 31, st = (k >> 5) & 3, patch = k >> 7;
+            const int ac = 4 * (patch >> 1) + (((lane >> 3) + st) & 3), rc = 32 * (patch & 1) + lane;
             if (is_w) {
-                const int a = k >> 6, rho = k & 63;
-                if (rho < nr && a < r) {
-                    const float v = sX[rho * L::LDX + a];
-                    X[(long long)a * rows + xb + rho] = v;
-                    Xb[(long long)a * ldb + xb + rho] = __float2bfloat16_rn(v);
+                if (rc < nr && ac < r) {
+                    const float v = sX[rc * L::LDX + ac];
+                    X[(long long)ac * rows + xb + rc] = v;
+                    Xb[(long long)ac * ldb + xb + rc] = __float2bfloat16_rn(v);
                 }
             } else {
                 const int rho = k / NP, a = k % NP;
                 if (rho < nr && a < r) X[(xb + rho) * r + a] = sX[rho * L::LDX + a];
-                const int a2 = k >> 6, rho2 = k & 63;
-                if (rho2 < nr && a2 < r) Xb[(long long)a2 * ldb + xb + rho2] = __float2bfloat16_rn(sX[rho2 * L::LDX + a2]);
+                if (rc < nr && ac < r) Xb[(long long)ac * ldb + xb + rc] = __float2bfloat16_rn(sX[rc * L::LDX + ac]);
             }
         }
         // this chunk's new rows into this CTA's Gram partial, rows in order
+        if constexpr (NP == 64) {
+            tg.add_rows(sX, L::LDX, nr);
+        } else {
 #pragma unroll 4
-        for (int rr = 0; rr < nr; rr++) {
-            float xa[GB], xb2[GB2];
-            lds_vec<GB>(sX + rr * L::LDX + ga0, xa);
-            lds_vec<GB2>(sX + rr * L::LDX + gb0, xb2);
+            for (int rr = 0; rr < nr; rr++) {
+                float xa[GB], xb2[GB2];
+                lds_vec<GB>(sX + rr * L::LDX + ga0, xa);
+                lds_vec<GB2>(sX + rr * L::LDX + gb0, xb2);
 #pragma unroll
-            for (int i = 0; i < GB; i++)
+                for (int i = 0; i < GB; i++)
 #pragma unroll
-                for (int k = 0; k < GB2; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
+                    for (int k = 0; k < GB2; k++) gacc[i][k] = fmaf(xa[i], xb2[k], gacc[i][k]);
+            }
         }
         if (tid == 0) {
             if (rd0 == last0) {
@@ -537,7 +657,9 @@ __device__ __forceinline__ void fused_tail(const SkParams &pr, int tid, float *s
     // this CTA's partial, packed (tri_stride): the thread's block holds G(ga, gb) for ga in
     // [ga0, ga0 + GB), gb in [gb0, gb0 + GB2); those with gb <= ga are entry (gb, ga), at
     // ga (ga + 1) / 2 + gb
-    if (ga0 + GB - 1 >= gb0) {
+    if constexpr (NP == 64) {
+        tg.store(gpc);
+    } else if (ga0 + GB - 1 >= gb0) {
 #pragma unroll
         for (int i = 0; i < GB; i++) {
             const int ga = ga0 + i;
