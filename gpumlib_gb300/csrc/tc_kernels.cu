@@ -1575,8 +1575,11 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
         }
     }
     if (p.update) {
-        // numerators: the tile's partial slots summed in slot order.  With the fixed-width slot
-        // table every load of every slot is independent, so they are all in flight at once.
+        // numerators: the tile's partial slots summed in slot order.  Rows lrow0 + c < 128 of a slot
+        // (RP == npad) are in bounds for every c < kUpdCols, so the loads need no column guard (the
+        // sums over the tile's padding rows are never stored).  The table lists a tile's slots
+        // first, then -1: four slots' loads are issued together (an absent slot reads the first one
+        // again and is not added); a branch around each slot's loads would serialise them.
         const int tile = c0 / 128, lrow0 = c0 % 128;
         constexpr int PER = kUpdCols * RP / kUpdThreads;
         float acc[PER];
@@ -1587,15 +1590,25 @@ __global__ void __launch_bounds__(kUpdThreads) tc_update_kernel(UpdParams p) {
             const int4 sa = ts[0], sb = ts[1];
             const int sl[kSlotW] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
 #pragma unroll
-            for (int q = 0; q < kSlotW; q++) {
-                if (sl[q] >= 0) {
-                    const float *base = p.P + ((size_t)sl[q] * 128 + lrow0) * p.npad;
+            for (int q0 = 0; q0 < kSlotW; q0 += 4) {
+                if (q0 > 0 && sl[q0] < 0) continue;
+                float v[4][PER];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int sq = sl[q0 + q] >= 0 ? sl[q0 + q] : sl[0];
+                    const float *base = p.P + ((size_t)sq * 128 + lrow0) * p.npad;
 #pragma unroll
                     for (int j = 0; j < PER; j++) {
                         const int k = tid + j * kUpdThreads, c = k / RP, a = k % RP;
-                        if (c < ncol) acc[j] += base[c * p.npad + a];
+                        v[q][j] = base[c * p.npad + a];
                     }
                 }
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (sl[q0 + q] >= 0) {
+#pragma unroll
+                        for (int j = 0; j < PER; j++) acc[j] += v[q][j];
+                    }
             }
         } else {
             const int s0 = p.slot_ptr[tile], s1 = p.slot_ptr[tile + 1];
