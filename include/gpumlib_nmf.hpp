@@ -19,8 +19,10 @@
  * draws W and H from a seeded counter-based generator (the reference uses
  * an unseeded rand(), nmf_base.h:56-61).
  * Additions: Residual() (FP64 relative Frobenius residual on the GPU), ObjectiveKL(),
- * Iterate(k), SetQualityInterval(k), and optional eps / precision
- * arguments on every constructor.
+ * Iterate(k), SetQualityInterval(k) (k > 0: every k-th iteration, 1 by default;
+ * 0: never; GPUNMF_QUALITY_WHEN_READY: the reference's rule, a sample whenever the
+ * previous read-back is complete), and optional eps / precision arguments on every
+ * constructor.
  */
 #ifndef GPUMLIB_GB300_NMF_HPP
 #define GPUMLIB_GB300_NMF_HPP
