@@ -48,6 +48,8 @@ FALLBACK_HBM_GBS = 6800.0
 FALLBACK_BF16_TFLOPS = 1900.0
 
 METRIC = "NMF iters/s, Euclidean multiplicative update, V 8192x8192, r=64"
+GENERATOR = (" (project generator, gpumlib_gb300/inputs.py: splitmix64 counters per element; Marsaglia-Tsang "
+             "gamma, Box-Muller normal, inversion / PTRS Poisson)")
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from the committed ncu
 # captures of this workload (one --set full capture per precision, see the profiles
@@ -381,7 +383,8 @@ def run_ours(args, rank, world, local, dist):
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if precision == "bf16" else "f32",
            "precision": precision,
-           "data": "synthetic: V = A B + |N(0,0.01)|, A,B ~ Gamma(2,0.5) (seed 2); W,H U[0,1)+1e-4 (seed 3)",
+           "data": "synthetic: V = A B + |N(0,0.01)|, A,B ~ Gamma(2,0.5) (seed 2); W,H U[0,1)+1e-4 (seed 3)"
+                   "%s" % GENERATOR,
            "config": workload_config(n, m, r, eps, world),
            "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roofline}
 
@@ -619,7 +622,8 @@ def run_batched(args, rank, world, local, dist):
     out = {"metric": BATCH_METRIC, "value": round(value, 1), "unit": "jobs/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic: per instance i (seed 1000+i) m~U{32..512}, n~U{32..1024}, r in {4,8,16,32}, V U[0,1)",
+           "data": "synthetic: per instance i (seed 1000+i) m~U{32..512}, n~U{32..1024}, r in {4,8,16,32}, V U[0,1)"
+                   "%s" % GENERATOR,
            "config": {"workload": "batched_%d_uneven_iters%d" % (count, iters), "instances": count,
                       "iters": iters, "rule": "euclidean", "precision": "fp32",
                       "l2": "each step re-reads every instance's V 2x per iteration; working set %.2f GB > L2" %
@@ -692,7 +696,7 @@ def run_kl(args, rank, world, local, dist):
            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if prec == "bf16" else "f32",
            "precision": prec,
            "data": "synthetic: V ~ Poisson(%sP Q), P 16384x128, Q 128x4096 ~ Gamma(0.3,1) (seed 4); W,H U[0,1)+1e-4 "
-                   "(seed 5)" % ("" if args.kl_lam_scale == 1.0 else "%g " % args.kl_lam_scale),
+                   "(seed 5)%s" % ("" if args.kl_lam_scale == 1.0 else "%g " % args.kl_lam_scale, GENERATOR),
            "config": workload_config(n, m, r, eps, world, rule="kl", lam_scale=args.kl_lam_scale,
                                      zero_fraction=round(float(np.mean(V == 0)), 5)),
            "clocks": clk.summary(), "timing": rep_info, "gpu_launches": t["launches"], "roofline": roof}
