@@ -220,3 +220,15 @@ def test_ctypes_signatures_match_header():
         for k, (p, a) in enumerate(zip(params, args)):
             assert _kind_of_c(p) == _kind_of_ctypes(a), (name, k, p, a)
         assert _kind_of_c(ret) == _kind_of_ctypes(res), (name, ret, res)
+
+
+def test_python_constants_match_header_macros():
+    """The Python mirror's constants are the header's values (the quality sampling mode, the rules,
+    the precisions)."""
+    import gpumlib_gb300 as g
+    text = open(os.path.join(ROOT, "include", "gpunmf.h")).read()
+    mt = re.search(r"#define\s+GPUNMF_QUALITY_WHEN_READY\s+\((-?\d+)\)", text)
+    assert mt and int(mt.group(1)) == g.QUALITY_WHEN_READY
+    values = {name: int(v) for name, v in re.findall(r"\b(GPUNMF_\w+)\s*=\s*(-?\d+)", text)}
+    assert values.get("GPUNMF_EUCLIDEAN") == g.EUCLIDEAN and values.get("GPUNMF_DIVERGENCE") == g.DIVERGENCE
+    assert values.get("GPUNMF_FP32") == g.nmf.PRECISIONS["fp32"] and values.get("GPUNMF_BF16") == g.nmf.PRECISIONS["bf16"]
