@@ -8,7 +8,7 @@ from gpumlib_gb300 import inputs
 pytestmark = pytest.mark.skipif(oracle.ref() is None, reason="reference HostNMF not built on this machine")
 
 
-@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("rule", [0, 1, 2, 3])
 @pytest.mark.parametrize("shape", [(19, 7, 2), (64, 64, 8), (130, 33, 11)])
 @pytest.mark.parametrize("updateW", [True, False])
 def test_reference_equals_oracle(rule, shape, updateW):
@@ -29,10 +29,11 @@ def same_bits(a, b):
 EDGE_SHAPES = [(1, 5, 1), (5, 1, 1), (17, 13, 1), (6, 4, 9), (2, 2, 2)]
 
 
-@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("rule", [0, 1, 2, 3])
 @pytest.mark.parametrize("shape", EDGE_SHAPES, ids=["%dx%dr%d" % s for s in EDGE_SHAPES])
 def test_reference_equals_oracle_edge_shapes(rule, shape):
-    """One row or column, rank 1, rank above both sides."""
+    """One row or column, rank 1, rank above both sides; the multiplicative (0, 1) and additive (2, 3)
+    rules of HostNMF.h:64-233."""
     n, m, r = shape
     V = inputs.uniform_matrix(300 + n, n, m)
     W, H = inputs.factors(400 + m, n, m, r)
@@ -41,7 +42,7 @@ def test_reference_equals_oracle_edge_shapes(rule, shape):
     assert same_bits(a[0], b[0]) and same_bits(a[1], b[1])
 
 
-@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("rule", [0, 1, 2, 3])
 def test_reference_equals_oracle_with_zeros(rule):
     """V with a zero row, a zero column and scattered exact zeros; W with a zero column (the CPU KL
     rule has no eps on its sums, so that column's H row becomes 0/0 there: NaN in both)."""
